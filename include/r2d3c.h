@@ -1,0 +1,204 @@
+/*
+ * r2d3c.h -- C-ABI of the GB300 (sm_103a) Rot2D3C time-step hot path.
+ *
+ * The reference (Fortran 90, MPI, FFTW 2) has no plugin system: its operator
+ * interface is the set of subroutines its main program calls.  Every entry
+ * point below names the reference routine it replaces (file:line, paths
+ * relative to the reference's src/).  A Fortran caller binds them with
+ * ISO_C_BINDING interface blocks; a Python caller with ctypes.
+ *
+ * Conventions
+ *   - Every function returns an int status: R2D3C_OK (0) or a negative code.
+ *     No exception or abort crosses the ABI.  r2d3c_last_error() gives text.
+ *   - Host buffers are caller-owned FP64 arrays in the reference's Fortran
+ *     layouts and are complete when the call returns:
+ *       spectral  C(n, n/2+1) complex*16, ky fastest  -> 2*n*(n/2+1) doubles,
+ *                 interleaved (re, im) (fftp2D.f90:153)
+ *       physical  R(n, n) real*8, x fastest           -> n*n doubles
+ *                 (fftp2D.f90:157)
+ *   - A context owns all device memory and one private CUDA stream.  It is
+ *     not thread-safe: use one context per host thread.  Distinct contexts may
+ *     run concurrently.
+ *   - Transforms are unnormalised with forward sign -1; a C2R(R2C(x)) round
+ *     trip returns n*n*x; C2R ignores Im at kx = 0 and kx = n/2 (FFTW).
+ *   - Supported grids: n = 16, 32, ..., 8192 (powers of two).
+ *   - Precision: R2D3C_FP64 computes everything in FP64 (the drop-in path);
+ *     R2D3C_FP32 keeps the fields and transforms in FP32 (compensated
+ *     twiddles) and every diagnostic reduction in FP64.
+ */
+#ifndef R2D3C_H
+#define R2D3C_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  R2D3C_OK = 0,
+  R2D3C_EINVAL = -1,   /* bad argument */
+  R2D3C_ECUDA = -2,    /* CUDA runtime error */
+  R2D3C_ENOMEM = -3,   /* device allocation failed */
+  R2D3C_ETIMEOUT = -4, /* a bounded device wait gave up */
+  R2D3C_EIO = -5,      /* file input/output error */
+  R2D3C_ESTATE = -6    /* call not valid in the current state */
+};
+
+enum { R2D3C_FP64 = 0, R2D3C_FP32 = 1 };
+
+/* FFT directions: FFTW_REAL_TO_COMPLEX (-1), FFTW_COMPLEX_TO_REAL (+1)
+   (fftw_f77.i:10-11). */
+enum { R2D3C_R2C = -1, R2D3C_C2R = 1 };
+
+/* time-step selection for r2d3c_advance */
+enum { R2D3C_DT_CFL = 0, R2D3C_DT_FIXED = 1 };
+
+/* field selection for r2d3c_get_field (Rot2D3C.para.f90:476-519) */
+enum { R2D3C_FIELD_PS = 0, R2D3C_FIELD_VZ = 1, R2D3C_FIELD_WW = 2, R2D3C_FIELD_INVLAP_PSI = 3 };
+
+/* The 25 positional values of parameter.inp (read at Rot2D3C.para.f90:136-160)
+   plus the grid size n (compile-time module grid in the reference,
+   pseudospec2D_mod.f90:101; a run-time value here). */
+typedef struct r2d3c_params {
+  int n;
+  double cfl;      /*  1 (commented "dt" in parameter.inp, read as CFL) */
+  int step;        /*  2 */
+  int cstep;       /*  3 */
+  int sstep;       /*  4 */
+  int tstep;       /*  5 */
+  double fp0;      /*  6 */
+  double fz0;      /*  7 */
+  double u0;       /*  8 */
+  double v0;       /*  9 */
+  double kdn;      /* 10 */
+  double kup;      /* 11 */
+  double nu;       /* 12 */
+  double hnu;      /* 13 */
+  int nn;          /* 14 */
+  int mm;          /* 15 */
+  double nuv;      /* 16 */
+  double hnuv;     /* 17 */
+  int nnv;         /* 18 */
+  int mmv;         /* 19 */
+  double omega;    /* 20 */
+  int seed;        /* 21 */
+  int iflow;       /* 22 */
+  double prm1;     /* 23 (unused by the reference) */
+  double prm2;     /* 24 (unused by the reference) */
+  double dt_corr;  /* 25 (unused by the reference) */
+} r2d3c_params;
+
+typedef struct r2d3c_ctx r2d3c_ctx;
+typedef struct r2d3c_plan r2d3c_plan;
+
+/* ---- library ---------------------------------------------------------- */
+const char* r2d3c_version(void);
+/* Text of the last error of any call on this host thread. */
+const char* r2d3c_last_error(void);
+/* Number of this library's kernels launched so far on this context. */
+int r2d3c_kernel_launches(const r2d3c_ctx* ctx, long long* count);
+
+/* ---- Level 1: layout-compatible 2-D FFT (fftp2D.f90) ------------------ */
+/* replaces fftp2d_create_plan (fftp2D.f90:30-63); flags (FFTW_ESTIMATE /
+   FFTW_MEASURE) are accepted and ignored. */
+int r2d3c_fft_plan_create(int n, int dir, int flags, int precision, r2d3c_plan** plan);
+/* replaces fftp2d_destroy_plan (fftp2D.f90:66-86) */
+int r2d3c_fft_plan_destroy(r2d3c_plan* plan);
+/* replaces fftp2d_real_to_complex (fftp2D.f90:133-211): in R(n,n) -> out C(n,n/2+1) */
+int r2d3c_fft_r2c(r2d3c_plan* plan, const double* in, double* out);
+/* replaces fftp2d_complex_to_real (fftp2D.f90:214-290): in C(n,n/2+1) -> out R(n,n).
+   The reference destroys its input; this one leaves it unchanged. */
+int r2d3c_fft_c2r(r2d3c_plan* plan, double* in, double* out);
+/* Same transforms on device FP64 buffers (same layouts) on `stream`
+   (a cudaStream_t, or NULL for the plan's stream); asynchronous. */
+int r2d3c_fft_r2c_dev(r2d3c_plan* plan, const double* d_in, double* d_out, void* stream);
+int r2d3c_fft_c2r_dev(r2d3c_plan* plan, const double* d_in, double* d_out, void* stream);
+
+/* ---- Level 2: the hot path -------------------------------------------- */
+/* Module state of the reference main program (Rot2D3C.para.f90:102-238):
+   wavenumbers, dealiasing bounds, plans and the state/forcing/work arrays. */
+int r2d3c_create(const r2d3c_params* params, int precision, r2d3c_ctx** ctx);
+int r2d3c_destroy(r2d3c_ctx* ctx);
+/* Bytes of device memory held by the context. */
+int r2d3c_device_bytes(const r2d3c_ctx* ctx, long long* bytes);
+
+/* State psi^, vz^ (spectral).  set_state marks the state "not truncated":
+   the next step applies the 2/3 truncation as the reference's first RK step
+   does (Rot2D3C.para.f90:578-611). */
+int r2d3c_set_state(r2d3c_ctx* ctx, const double* ps_hat, const double* vz_hat);
+int r2d3c_get_state(r2d3c_ctx* ctx, double* ps_hat, double* vz_hat);
+/* Restart path (Rot2D3C.para.f90:322-329): physical psi, vz -> R2C, no mask. */
+int r2d3c_set_state_physical(r2d3c_ctx* ctx, const double* ps, const double* vz);
+/* Forcing fp^, fz^ (spectral). */
+int r2d3c_set_forcing(r2d3c_ctx* ctx, const double* fp_hat, const double* fz_hat);
+int r2d3c_get_forcing(r2d3c_ctx* ctx, double* fp_hat, double* fz_hat);
+
+/* Seeded initial condition, stat == 0 branch (Rot2D3C.para.f90:245-299).
+   *seed is advanced exactly as the reference's randu calls advance it. */
+int r2d3c_initial_conditions(r2d3c_ctx* ctx, int* seed);
+/* Forcing set-up before the loop by iflow (Rot2D3C.para.f90:343-381):
+   iflow 1 deterministic, 2 const_inj, 3 CFL + rand_force.  Seeds advance as
+   in the reference; *seed1 receives seed+1 (and its advanced value). */
+int r2d3c_forcing_init(r2d3c_ctx* ctx, int* seed, int* seed1);
+
+/* replaces CFL_condition (pseudospec2D_Rot2D3C.f90:840-899) */
+int r2d3c_cfl(r2d3c_ctx* ctx, double cfl, double* dt);
+/* replaces the two rand_force calls of one step (Rot2D3C.para.f90:413-416,
+   pseudospec2D_Rot2D3C.f90:1063-1126) with the given dt */
+int r2d3c_force_random(r2d3c_ctx* ctx, double dt, int* seed, int* seed1);
+/* One RK step of order 4 (Rot2D3C.para.f90:545-611) with the given dt.
+   For iflow == 2 the forcing is rebuilt by const_inj at every substep
+   (:565-569) and *seed, *seed1 advance as in the reference. */
+int r2d3c_step(r2d3c_ctx* ctx, double dt, int* seed, int* seed1);
+/* nsteps iterations of the main loop body without diagnostics
+   (Rot2D3C.para.f90:399, :413-416, :537, :545-611): dt from the CFL condition
+   (dt_mode R2D3C_DT_CFL, cfl_or_dt = CFL factor) or fixed (R2D3C_DT_FIXED),
+   rand_force every step when iflow == 3, time += dt.  One step is captured in
+   a CUDA graph and replayed.  On return *time and *dt_last hold the device
+   values (either may be NULL). */
+int r2d3c_advance(r2d3c_ctx* ctx, int nsteps, int dt_mode, double cfl_or_dt, double* time,
+                  double* dt_last, int* seed, int* seed1);
+int r2d3c_set_time(r2d3c_ctx* ctx, double time);
+
+/* replaces cond_check (pseudospec2D_Rot2D3C.f90:455-612): the 30 values the
+   reference appends to energy_bal.txt (12), enstrophy_bal.txt (5),
+   helicity_bal.txt (8) and max_min.txt (5), in file order. */
+int r2d3c_cond_check(r2d3c_ctx* ctx, double time, double out[30]);
+/* replaces spectrum (:615-712): Ek, Ezk with n/2+1 shells each */
+int r2d3c_spectrum(r2d3c_ctx* ctx, double* Ek, double* Ezk);
+/* replaces transfers (:715-837): per-shell Fl0, Fl1, Fl2 (n/2+1 each);
+   fluxes are their running sums (:824-830) */
+int r2d3c_transfers(r2d3c_ctx* ctx, double* Fl0, double* Fl1, double* Fl2);
+/* Field output of Rot2D3C.para.f90:476-519 (ps, vz, ww, invlap_psi), each
+   scaled by 1/n^2 before the C2R, as R(n,n). */
+int r2d3c_get_field(r2d3c_ctx* ctx, int which, double* R);
+
+/* ---- Level 2 operators (reference subroutines on host arrays) ---------- */
+/* derivk2 (pseudospec2D_Rot2D3C.f90:6-68) */
+int r2d3c_derivk2(r2d3c_ctx* ctx, const double* a, double* b, int dir);
+/* laplak2 (:71-95) */
+int r2d3c_laplak2(r2d3c_ctx* ctx, const double* a, double* b);
+/* inv_laplak2 (:98-127) */
+int r2d3c_inv_laplak2(r2d3c_ctx* ctx, const double* a, double* b);
+/* poisson (:169-226) */
+int r2d3c_poisson(r2d3c_ctx* ctx, const double* a, const double* b, double* c);
+/* energy (:336-396) */
+int r2d3c_energy(r2d3c_ctx* ctx, const double* a, int kin, double* b);
+/* inerprod (:400-451) */
+int r2d3c_inerprod(r2d3c_ctx* ctx, const double* a, const double* b, int kin, double* rslt);
+/* randu (pseudospec2D_mod.f90:142-161): one draw, *seed updated */
+float r2d3c_randu(int* seed);
+
+/* Device pointer of a context plane for GPU-resident callers:
+   which = 0 ps, 1 vz, 2 fp, 3 fz (spectral planes of the context's compute
+   type, complex interleaved [kx][ky]). */
+int r2d3c_dev_ptr(r2d3c_ctx* ctx, int which, void** ptr);
+/* The context's CUDA stream (cudaStream_t). */
+int r2d3c_stream(r2d3c_ctx* ctx, void** stream);
+/* Block until all queued work of the context is done. */
+int r2d3c_synchronize(r2d3c_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* R2D3C_H */

@@ -1,0 +1,682 @@
+// C-ABI of the Rot2D3C GB300 hot path (declared in include/r2d3c.h).
+//
+// Host-side logic that the reference keeps in Fortran and that is not device
+// work lives here: parameter checks, the randu generator and the forcing
+// draws, the order of the reference's calls inside each entry point, and the
+// mapping of errors to status codes.  Device work goes to the engine of the
+// context (r2d3c_engine_impl.cuh).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/r2d3c.h"
+#include "r2d3c_engine.h"
+
+namespace r2d3c {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  cudaGetLastError();
+  const int code = (e == cudaErrorMemoryAllocation) ? kENOMEM : kECUDA;
+  throw Error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool supported_n(int n) { return n >= 16 && n <= 8192 && (n & (n - 1)) == 0; }
+
+}  // namespace r2d3c
+
+using namespace r2d3c;
+
+namespace {
+
+thread_local std::string g_err;
+void set_err(const std::string& s) { g_err = s; }
+
+constexpr double kPi = 3.1415926535897932384;  // module var (pseudospec2D_mod.f90:125)
+
+// randu (pseudospec2D_mod.f90:142-161): XOR-masked Park-Miller step with
+// Schrage's factorisation in 32-bit integers; REAL (float) arithmetic for the
+// result.  *idum is updated in place like the Fortran INTEGER argument.
+float randu_impl(int* idum) {
+  const int iq = 127773, ir = 2836, mask = 123459876;
+  const int ia = 16807, im = 2147483647;
+  const float am = 1.0f / (float)im;  // REAL parameter am = 1./im
+  int s = *idum ^ mask;
+  const int k = s / iq;  // truncates toward zero, as Fortran INTEGER division
+  const long long t = (long long)ia * (long long)(s - k * iq) - (long long)ir * k;
+  s = (int)(unsigned)(unsigned long long)t;  // 32-bit two's-complement wrap
+  if (s < 0) s += im;
+  float r = am * (float)s;
+  r = (r - 0.5f) * 2.0f;
+  *idum = s ^ mask;
+  return r;
+}
+
+double ipow(double x, int k) {  // REAL**INTEGER by repeated squaring
+  if (k == 0) return 1.0;
+  unsigned e = k < 0 ? (unsigned)(-k) : (unsigned)k;
+  double r = 1.0, b = x;
+  while (true) {
+    if (e & 1u) r = r * b;
+    e >>= 1;
+    if (!e) break;
+    b = b * b;
+  }
+  return k < 0 ? 1.0 / r : r;
+}
+
+}  // namespace
+
+struct r2d3c_ctx {
+  r2d3c_params p{};
+  std::unique_ptr<IEngine> eng;
+  int ci_final_seed = 0;  // seed value left by one const_inj call
+  ModelCoef mc() const { return ModelCoef{p.nu, p.hnu, p.nuv, p.hnuv, p.omega, p.nn, p.mm, p.nnv, p.mmv}; }
+};
+
+struct r2d3c_plan {
+  int n = 0, dir = 0;
+  std::unique_ptr<IEngine> eng;
+};
+
+#define API_BEGIN try {
+#define API_END                                                  \
+  }                                                              \
+  catch (const Error& e) {                                       \
+    set_err(e.what());                                           \
+    return e.code;                                               \
+  }                                                              \
+  catch (const std::bad_alloc&) {                                \
+    set_err("host allocation failed");                           \
+    return R2D3C_ENOMEM;                                         \
+  }                                                              \
+  catch (const std::exception& e) {                              \
+    set_err(e.what());                                           \
+    return R2D3C_EINVAL;                                         \
+  }                                                              \
+  catch (...) {                                                  \
+    set_err("unknown error");                                    \
+    return R2D3C_EINVAL;                                         \
+  }                                                              \
+  return R2D3C_OK;
+
+#define REQUIRE(cond, msg)                   \
+  do {                                       \
+    if (!(cond)) throw Error(kEINVAL, msg);  \
+  } while (0)
+
+namespace {
+
+IEngine* new_engine(int n, int precision, bool full) {
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  return precision == R2D3C_FP64 ? make_engine_f64(n, dev, full) : make_engine_f32(n, dev, full);
+}
+
+// One rand_force draw (pseudospec2D_Rot2D3C.f90:1086-1099, one rank): the
+// mode (kx, ky) of length kup, the phase, and the entries it sets
+// (:1100-1122).  *seed advances by one randu call; the phase uses the
+// temporary seed+1.
+RandForceHost rand_force_draw(const r2d3c_params& p, double f0, int kin, int* seed) {
+  const int n = p.n;
+  const double theta = (double)randu_impl(seed) * kPi;
+  int tmpseed = *seed + 1;
+  const double phase = (double)randu_impl(&tmpseed) * kPi;
+  const double kx = std::floor(p.kup * std::cos(theta) + 0.5);
+  const double ky = std::floor(p.kup * std::sin(theta) + 0.5);
+  RandForceHost f{};
+  f.c0 = std::sqrt(2.0 * f0);
+  f.kpow = ipow(p.kup, kin);
+  f.cph = std::cos(phase);
+  f.sph = std::sin(phase);
+  auto ka = [n](int j) { return (double)(j < n / 2 ? j : j - n); };
+  auto add = [&f](int idx, int cj) {
+    if (f.nset < 4) {
+      f.set[f.nset] = idx;
+      f.conj[f.nset] = cj;
+      ++f.nset;
+    }
+  };
+  for (int i = 1; i <= n / 2; ++i) {  // columns i != 1 of the reference
+    const double kai = ka(i);
+    if (kai == ky || kai == -ky)
+      for (int j = 0; j < n; ++j)
+        if (ka(j) == kx) add(i * n + j, 0);
+  }
+  if (ky == 0.0)  // column i = 1 (kx = 0), :1109-1121
+    for (int j = 1; j < n / 2; ++j)
+      if (ka(j) == kx) {
+        add(j, 0);
+        add(n - j, 1);
+      }
+  return f;
+}
+
+void rand_force_pair(r2d3c_ctx* c, int* seed, int* seed1, RandForceHost out[2]) {
+  out[0] = rand_force_draw(c->p, c->p.fp0, 1, seed);   // fp with seed (:414)
+  out[1] = rand_force_draw(c->p, c->p.fz0, 0, seed1);  // fz with seed1 (:415)
+}
+
+// Band list of const_inj in the reference's loop order (kx = 0 column first,
+// j = 2..n/2; then columns 2..n/2+1, j = 1..n), its kx = 0 mirrors and the
+// randu factors drawn from the seed myrank = 0 (:1032-1057).
+void setup_const_inj(r2d3c_ctx* c, bool on) {
+  const int n = c->p.n;
+  const double lo = c->p.kdn * c->p.kdn, hi = c->p.kup * c->p.kup;
+  auto ka = [n](int j) { return (double)(j < n / 2 ? j : j - n); };
+  std::vector<int> idx, mir;
+  std::vector<float> rnd;
+  int s = 0;  // seed1 = myrank
+  for (int j = 1; j < n / 2; ++j) {
+    const double k2 = ka(j) * ka(j);
+    if (k2 <= hi && k2 >= lo) {
+      idx.push_back(j);
+      mir.push_back(n - j);
+      rnd.push_back(randu_impl(&s));
+    }
+  }
+  for (int i = 1; i <= n / 2; ++i)
+    for (int j = 0; j < n; ++j) {
+      const double k2 = ka(i) * ka(i) + ka(j) * ka(j);
+      if (k2 <= hi && k2 >= lo) {
+        idx.push_back(i * n + j);
+        mir.push_back(-1);
+        rnd.push_back(randu_impl(&s));
+      }
+    }
+  c->ci_final_seed = s;
+  c->eng->set_const_inj(on, c->p.kdn, c->p.kup, c->p.fp0, c->p.fz0, idx, mir, rnd);
+}
+
+void check_params(const r2d3c_params* p) {
+  REQUIRE(p, "params is NULL");
+  REQUIRE(supported_n(p->n), "n must be a power of two in [16, 8192]");
+  REQUIRE(p->nn >= -64 && p->nn <= 64 && p->mm >= -64 && p->mm <= 64 && p->nnv >= -64 &&
+              p->nnv <= 64 && p->mmv >= -64 && p->mmv <= 64,
+          "dissipation orders out of range");
+  REQUIRE(p->iflow >= 0 && p->iflow <= 3, "iflow must be 0..3");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* r2d3c_version(void) { return "rot2d3c_gb300 0.1 (sm_103a)"; }
+const char* r2d3c_last_error(void) { return g_err.c_str(); }
+float r2d3c_randu(int* seed) { return seed ? randu_impl(seed) : 0.0f; }
+
+int r2d3c_kernel_launches(const r2d3c_ctx* ctx, long long* count) {
+  API_BEGIN
+  REQUIRE(ctx && count, "NULL argument");
+  *count = ctx->eng->kernel_launches();
+  API_END
+}
+
+// ---------------------------------------------------------------- Level 1
+int r2d3c_fft_plan_create(int n, int dir, int flags, int precision, r2d3c_plan** plan) {
+  (void)flags;
+  API_BEGIN
+  REQUIRE(plan, "plan is NULL");
+  *plan = nullptr;
+  REQUIRE(supported_n(n), "n must be a power of two in [16, 8192]");
+  REQUIRE(dir == R2D3C_R2C || dir == R2D3C_C2R, "dir must be -1 (R2C) or +1 (C2R)");
+  REQUIRE(precision == R2D3C_FP64 || precision == R2D3C_FP32, "bad precision");
+  std::unique_ptr<r2d3c_plan> pl(new r2d3c_plan());
+  pl->n = n;
+  pl->dir = dir;
+  pl->eng.reset(new_engine(n, precision, false));
+  *plan = pl.release();
+  API_END
+}
+
+int r2d3c_fft_plan_destroy(r2d3c_plan* plan) {
+  API_BEGIN
+  delete plan;
+  API_END
+}
+
+int r2d3c_fft_r2c(r2d3c_plan* plan, const double* in, double* out) {
+  API_BEGIN
+  REQUIRE(plan && in && out, "NULL argument");
+  REQUIRE(plan->dir == R2D3C_R2C, "plan direction is not R2C");
+  plan->eng->upload_real(R_1, in);
+  plan->eng->r2c(R_1, P_W1);
+  plan->eng->download_spec(P_W1, out);
+  API_END
+}
+
+int r2d3c_fft_c2r(r2d3c_plan* plan, double* in, double* out) {
+  API_BEGIN
+  REQUIRE(plan && in && out, "NULL argument");
+  REQUIRE(plan->dir == R2D3C_C2R, "plan direction is not C2R");
+  plan->eng->upload_spec(P_W1, in);
+  plan->eng->c2r(P_W1, R_1, nullptr, nullptr);
+  plan->eng->download_real(R_1, out);
+  API_END
+}
+
+namespace {
+// order the plan's stream after `user` and `user` after the plan's work
+struct StreamJoin {
+  cudaStream_t user, own;
+  cudaEvent_t ev = nullptr;
+  StreamJoin(void* u, cudaStream_t o) : user((cudaStream_t)u), own(o) {
+    if (user && user != own) {
+      cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+      cuda_check(cudaEventRecord(ev, user), "cudaEventRecord");
+      cuda_check(cudaStreamWaitEvent(own, ev, 0), "cudaStreamWaitEvent");
+    }
+  }
+  void done() {
+    if (ev) {
+      cuda_check(cudaEventRecord(ev, own), "cudaEventRecord");
+      cuda_check(cudaStreamWaitEvent(user, ev, 0), "cudaStreamWaitEvent");
+    }
+  }
+  ~StreamJoin() {
+    if (ev) cudaEventDestroy(ev);
+  }
+};
+}  // namespace
+
+int r2d3c_fft_r2c_dev(r2d3c_plan* plan, const double* d_in, double* d_out, void* stream) {
+  API_BEGIN
+  REQUIRE(plan && d_in && d_out, "NULL argument");
+  REQUIRE(plan->dir == R2D3C_R2C, "plan direction is not R2C");
+  StreamJoin j(stream, plan->eng->stream());
+  plan->eng->real_from_dev64(R_1, d_in);
+  plan->eng->r2c(R_1, P_W1);
+  plan->eng->spec_to_dev64(P_W1, d_out);
+  j.done();
+  API_END
+}
+
+int r2d3c_fft_c2r_dev(r2d3c_plan* plan, const double* d_in, double* d_out, void* stream) {
+  API_BEGIN
+  REQUIRE(plan && d_in && d_out, "NULL argument");
+  REQUIRE(plan->dir == R2D3C_C2R, "plan direction is not C2R");
+  StreamJoin j(stream, plan->eng->stream());
+  plan->eng->spec_from_dev64(P_W1, d_in);
+  plan->eng->c2r(P_W1, R_1, nullptr, nullptr);
+  plan->eng->real_to_dev64(R_1, d_out);
+  j.done();
+  API_END
+}
+
+// ---------------------------------------------------------------- Level 2
+int r2d3c_create(const r2d3c_params* params, int precision, r2d3c_ctx** ctx) {
+  API_BEGIN
+  REQUIRE(ctx, "ctx is NULL");
+  *ctx = nullptr;
+  check_params(params);
+  REQUIRE(precision == R2D3C_FP64 || precision == R2D3C_FP32, "bad precision");
+  std::unique_ptr<r2d3c_ctx> c(new r2d3c_ctx());
+  c->p = *params;
+  c->eng.reset(new_engine(params->n, precision, true));
+  if (params->iflow == 2) setup_const_inj(c.get(), true);
+  *ctx = c.release();
+  API_END
+}
+
+int r2d3c_destroy(r2d3c_ctx* ctx) {
+  API_BEGIN
+  delete ctx;
+  API_END
+}
+
+int r2d3c_device_bytes(const r2d3c_ctx* ctx, long long* bytes) {
+  API_BEGIN
+  REQUIRE(ctx && bytes, "NULL argument");
+  *bytes = (long long)ctx->eng->bytes_allocated();
+  API_END
+}
+
+int r2d3c_set_state(r2d3c_ctx* ctx, const double* ps_hat, const double* vz_hat) {
+  API_BEGIN
+  REQUIRE(ctx && ps_hat && vz_hat, "NULL argument");
+  ctx->eng->upload_spec(P_PS, ps_hat);
+  ctx->eng->upload_spec(P_VZ, vz_hat);
+  ctx->eng->mark_state_untruncated();
+  API_END
+}
+
+int r2d3c_get_state(r2d3c_ctx* ctx, double* ps_hat, double* vz_hat) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  if (ps_hat) ctx->eng->download_spec(P_PS, ps_hat);
+  if (vz_hat) ctx->eng->download_spec(P_VZ, vz_hat);
+  API_END
+}
+
+int r2d3c_set_state_physical(r2d3c_ctx* ctx, const double* ps, const double* vz) {
+  API_BEGIN
+  REQUIRE(ctx && ps && vz, "NULL argument");
+  ctx->eng->upload_real(R_1, ps);
+  ctx->eng->r2c(R_1, P_PS);  // :324-325
+  ctx->eng->upload_real(R_1, vz);
+  ctx->eng->r2c(R_1, P_VZ);  // :328-329
+  ctx->eng->mark_state_untruncated();
+  ctx->eng->sync();
+  API_END
+}
+
+int r2d3c_set_forcing(r2d3c_ctx* ctx, const double* fp_hat, const double* fz_hat) {
+  API_BEGIN
+  REQUIRE(ctx && fp_hat && fz_hat, "NULL argument");
+  ctx->eng->upload_spec(P_FP, fp_hat);
+  ctx->eng->upload_spec(P_FZ, fz_hat);
+  API_END
+}
+
+int r2d3c_get_forcing(r2d3c_ctx* ctx, double* fp_hat, double* fz_hat) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  if (fp_hat) ctx->eng->download_spec(P_FP, fp_hat);
+  if (fz_hat) ctx->eng->download_spec(P_FZ, fz_hat);
+  API_END
+}
+
+namespace {
+double energy_of(IEngine* e, int plane, int kin) {
+  const int kind = 0 /* S_ENERGY */, ia = 0, ib = 0;
+  const int pl[4] = {plane, -1, -1, -1};
+  double out = 0.0;
+  e->halfplane_sums(1, &kind, &ia, &ib, &kin, 0.0, 0.0, pl, &out);
+  return out;
+}
+}  // namespace
+
+int r2d3c_initial_conditions(r2d3c_ctx* ctx, int* seed) {
+  API_BEGIN
+  REQUIRE(ctx && seed, "NULL argument");
+  const r2d3c_params& p = ctx->p;
+  std::vector<IcModeHost> modes;
+  const int kend = (int)(p.kup + 1);  // DO ir = 1,kup+1 with kup DOUBLE
+  for (int ir = 1; ir <= kend; ++ir)
+    for (int jr = 1; jr <= kend; ++jr) {
+      IcModeHost m{};
+      m.ir = ir;
+      m.jr = jr;
+      m.kr = std::sqrt((double)(ir * ir + jr * jr));
+      m.ph1 = (double)randu_impl(seed) * 2.0 * kPi;
+      m.ph2 = (double)randu_impl(seed) * 2.0 * kPi;
+      m.ph3 = (double)randu_impl(seed) * 2.0 * kPi;
+      m.ph4 = (double)randu_impl(seed) * 2.0 * kPi;
+      modes.push_back(m);
+    }
+  IEngine* e = ctx->eng.get();
+  e->initial_condition_phys(modes);  // :255-279
+  e->r2c(R_1, P_PS);                 // :280
+  e->r2c(R_2, P_VZ);                 // :281
+  const double ener = energy_of(e, P_PS, 1);
+  const double enerv = energy_of(e, P_VZ, 0);
+  e->scale_mask2(P_PS, P_VZ, p.u0 / std::sqrt(ener), p.v0 / std::sqrt(enerv));  // :286-298
+  e->sync();
+  API_END
+}
+
+int r2d3c_forcing_init(r2d3c_ctx* ctx, int* seed, int* seed1) {
+  API_BEGIN
+  REQUIRE(ctx && seed && seed1, "NULL argument");
+  r2d3c_params& p = ctx->p;
+  IEngine* e = ctx->eng.get();
+  if (p.iflow == 1) {  // :343-371
+    p.kdn = p.kup;
+    e->iflow1_phys(p.kup);
+    e->r2c(R_1, P_FP);
+    const double eneru = energy_of(e, P_FP, 1);
+    e->r2c(R_2, P_FZ);
+    const double enerv = energy_of(e, P_FZ, 0);
+    e->scale_mask2(P_FP, P_FZ, p.fp0 / std::sqrt(eneru), p.fz0 / std::sqrt(enerv));
+  } else if (p.iflow == 2) {  // :372-375
+    *seed1 = *seed + 1;
+    e->const_inj(P_PS, P_FP, 1, p.fp0);
+    e->const_inj(P_VZ, P_FZ, 0, p.fz0);
+    *seed1 = ctx->ci_final_seed;
+    *seed = ctx->ci_final_seed;
+  } else if (p.iflow == 3) {  // :376-380
+    *seed1 = *seed + 1;
+    e->cfl(p.cfl, ctx->mc());
+    RandForceHost f[2];
+    rand_force_pair(ctx, seed, seed1, f);
+    e->rand_force(f);
+  } else {
+    e->zero_spec(P_FP);
+    e->zero_spec(P_FZ);
+  }
+  e->sync();
+  API_END
+}
+
+int r2d3c_cfl(r2d3c_ctx* ctx, double cfl, double* dt) {
+  API_BEGIN
+  REQUIRE(ctx && dt, "NULL argument");
+  *dt = ctx->eng->cfl(cfl, ctx->mc());
+  API_END
+}
+
+int r2d3c_force_random(r2d3c_ctx* ctx, double dt, int* seed, int* seed1) {
+  API_BEGIN
+  REQUIRE(ctx && seed && seed1, "NULL argument");
+  REQUIRE(dt > 0.0, "dt must be positive");
+  ctx->eng->set_dt(dt);
+  RandForceHost f[2];
+  rand_force_pair(ctx, seed, seed1, f);
+  ctx->eng->rand_force(f);
+  ctx->eng->sync();
+  API_END
+}
+
+int r2d3c_step(r2d3c_ctx* ctx, double dt, int* seed, int* seed1) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  REQUIRE(dt > 0.0 && std::isfinite(dt), "dt must be positive and finite");
+  ctx->eng->set_dt(dt);
+  ctx->eng->step(ctx->mc(), false, 0.0, false, nullptr);
+  if (ctx->p.iflow == 2 && seed && seed1) *seed = *seed1 = ctx->ci_final_seed;
+  ctx->eng->sync();
+  API_END
+}
+
+int r2d3c_advance(r2d3c_ctx* ctx, int nsteps, int dt_mode, double cfl_or_dt, double* time,
+                  double* dt_last, int* seed, int* seed1) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  REQUIRE(nsteps >= 0, "nsteps must be >= 0");
+  REQUIRE(dt_mode == R2D3C_DT_CFL || dt_mode == R2D3C_DT_FIXED, "bad dt_mode");
+  REQUIRE(cfl_or_dt > 0.0 && std::isfinite(cfl_or_dt), "cfl_or_dt must be positive and finite");
+  IEngine* e = ctx->eng.get();
+  std::vector<RandForceHost> rf;
+  if (ctx->p.iflow == 3) {
+    REQUIRE(seed && seed1, "iflow 3 needs seed and seed1");
+    rf.resize(2 * (size_t)nsteps);
+    for (int s = 0; s < nsteps; ++s) rand_force_pair(ctx, seed, seed1, &rf[2 * (size_t)s]);
+  }
+  if (dt_mode == R2D3C_DT_FIXED) e->set_dt(cfl_or_dt);
+  e->advance(ctx->mc(), nsteps, dt_mode == R2D3C_DT_CFL, cfl_or_dt, rf.empty() ? nullptr : rf.data());
+  if (ctx->p.iflow == 2 && seed && seed1 && nsteps > 0) *seed = *seed1 = ctx->ci_final_seed;
+  if (time) *time = e->get_time();
+  if (dt_last) *dt_last = e->get_dt();
+  e->sync();
+  API_END
+}
+
+int r2d3c_set_time(r2d3c_ctx* ctx, double time) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  ctx->eng->set_time(time);
+  API_END
+}
+
+int r2d3c_cond_check(r2d3c_ctx* ctx, double time, double out[30]) {
+  API_BEGIN
+  REQUIRE(ctx && out, "NULL argument");
+  const r2d3c_params& p = ctx->p;
+  IEngine* e = ctx->eng.get();
+  // slots 0 ps, 1 vz, 2 fp, 3 fz; kinds: 0 energy, 1 inerprod, 2 inerprod(a, d_y b),
+  // 3 band ka2|a|^2, 4 band |a|^2   (pseudospec2D_Rot2D3C.f90:484-568)
+  const int kind[22] = {0, 1, 0, 0, 0, 1, 0, 0, 2, 0, 1, 0, 0, 1, 1, 1, 1, 1, 1, 1, 3, 4};
+  const int ia[22] = {0, 0, 0, 0, 1, 1, 1, 1, 1, 0, 0, 0, 0, 1, 1, 0, 1, 1, 0, 0, 0, 1};
+  const int ib[22] = {0, 2, 0, 0, 1, 3, 1, 1, 0, 0, 2, 0, 0, 0, 2, 3, 0, 0, 1, 1, 0, 1};
+  const int kin[22] = {1,          1,          p.nn + 1,   1 - p.mm,   0, 0, p.nnv, -p.mmv,
+                       0,          2,          2,          p.nn + 2,   2 - p.mm, 1, 1, 1,
+                       p.nn + 1,   1 - p.mm,   p.nnv + 1,  1 - p.mmv,  0, 0};
+  const int planes[4] = {P_PS, P_VZ, P_FP, P_FZ};
+  double s[22];
+  const double band_hi = 2.01 * p.kup * p.kup, band_lo = p.kup * p.kup;
+  e->halfplane_sums(22, kind, ia, ib, kin, band_lo, band_hi, planes, s);
+  const double Ep1 = s[0], injp1 = s[1], Dsp = s[2], Hds = s[3], Epv = s[4], injz = s[5];
+  const double Dspv = s[6], Hdsv = s[7], coup = s[8], Ep2 = s[9], injp2 = s[10], Dspw = s[11];
+  const double Hdsw = s[12], Eph = s[13], injh1 = s[14], injh2 = s[15], Dsph1 = s[16];
+  const double Hdsh1 = s[17], Dsph2 = s[18], Hdsh2 = s[19], Efp = s[20], Efpz = s[21];
+  double maxw, minw, maxv, minv;
+  e->specop(P_PS, P_W1, 3 /* laplak2 */, 0.0);  // :573-576
+  e->c2r(P_W1, -1, &maxw, &minw);
+  e->specop(P_VZ, P_W1, 0 /* derivk2 dir 0 */, 0.0);  // :581-584
+  e->c2r(P_W1, -1, &maxv, &minv);
+  const double w2 = 2 * p.omega;
+  const double v[30] = {time, Ep1, Epv, injp1, injz, p.nu * Dsp, p.nuv * Dspv, p.hnu * Hds,
+                        p.hnuv * Hdsv, w2 * coup, Efp, Efpz,
+                        time, Ep2, injp2, p.nu * Dspw, p.hnu * Hdsw,
+                        time, -Eph, -injh1, -injh2, -p.nu * Dsph1, -p.nuv * Dsph2, -p.hnu * Hdsh1,
+                        -p.hnuv * Hdsh2,
+                        time, maxw, minw, maxv, minv};
+  std::memcpy(out, v, sizeof(v));
+  API_END
+}
+
+int r2d3c_spectrum(r2d3c_ctx* ctx, double* Ek, double* Ezk) {
+  API_BEGIN
+  REQUIRE(ctx && Ek && Ezk, "NULL argument");
+  const int nb = ctx->p.n / 2 + 1;
+  std::vector<double> o5((size_t)nb * 5);
+  ctx->eng->shells(false, o5.data());
+  for (int b = 0; b < nb; ++b) {
+    Ek[b] = o5[(size_t)b * 5 + 0];
+    Ezk[b] = o5[(size_t)b * 5 + 1];
+  }
+  API_END
+}
+
+int r2d3c_transfers(r2d3c_ctx* ctx, double* Fl0, double* Fl1, double* Fl2) {
+  API_BEGIN
+  REQUIRE(ctx && Fl0 && Fl1 && Fl2, "NULL argument");
+  const int nb = ctx->p.n / 2 + 1;
+  std::vector<double> o5((size_t)nb * 5);
+  ctx->eng->shells(true, o5.data());
+  for (int b = 0; b < nb; ++b) {
+    Fl0[b] = o5[(size_t)b * 5 + 2];
+    Fl1[b] = o5[(size_t)b * 5 + 3];
+    Fl2[b] = o5[(size_t)b * 5 + 4];
+  }
+  API_END
+}
+
+int r2d3c_get_field(r2d3c_ctx* ctx, int which, double* R) {
+  API_BEGIN
+  REQUIRE(ctx && R, "NULL argument");
+  REQUIRE(which >= 0 && which <= 3, "bad field selector");
+  IEngine* e = ctx->eng.get();
+  const double n = (double)ctx->p.n;
+  const double tmp = 1.0 / (n * n);  // :476
+  switch (which) {
+    case R2D3C_FIELD_PS: e->specop(P_PS, P_W1, 5, tmp); break;
+    case R2D3C_FIELD_VZ: e->specop(P_VZ, P_W1, 5, tmp); break;
+    case R2D3C_FIELD_WW: e->specop(P_PS, P_W1, 6, tmp); break;
+    default:
+      e->specop(P_PS, P_W2, 4, 0.0);  // inv_laplak2 (:509)
+      e->specop(P_W2, P_W1, 5, tmp);
+      break;
+  }
+  e->c2r(P_W1, R_1, nullptr, nullptr);
+  e->download_real(R_1, R);
+  API_END
+}
+
+// ---------------------------------------------------------------- operators
+int r2d3c_derivk2(r2d3c_ctx* ctx, const double* a, double* b, int dir) {
+  API_BEGIN
+  REQUIRE(ctx && a && b, "NULL argument");
+  REQUIRE(dir >= 0 && dir <= 2, "dir must be 0, 1 or 2");
+  ctx->eng->upload_spec(P_C1, a);
+  ctx->eng->specop(P_C1, P_C2, dir, 0.0);
+  ctx->eng->download_spec(P_C2, b);
+  API_END
+}
+
+int r2d3c_laplak2(r2d3c_ctx* ctx, const double* a, double* b) {
+  API_BEGIN
+  REQUIRE(ctx && a && b, "NULL argument");
+  ctx->eng->upload_spec(P_C1, a);
+  ctx->eng->specop(P_C1, P_C2, 3, 0.0);
+  ctx->eng->download_spec(P_C2, b);
+  API_END
+}
+
+int r2d3c_inv_laplak2(r2d3c_ctx* ctx, const double* a, double* b) {
+  API_BEGIN
+  REQUIRE(ctx && a && b, "NULL argument");
+  ctx->eng->upload_spec(P_C1, a);
+  ctx->eng->specop(P_C1, P_C2, 4, 0.0);
+  ctx->eng->download_spec(P_C2, b);
+  API_END
+}
+
+int r2d3c_poisson(r2d3c_ctx* ctx, const double* a, const double* b, double* c) {
+  API_BEGIN
+  REQUIRE(ctx && a && b && c, "NULL argument");
+  ctx->eng->upload_spec(P_C1, a);
+  ctx->eng->upload_spec(P_C2, b);
+  ctx->eng->poisson(P_C1, P_C2, P_B5);
+  ctx->eng->download_spec(P_B5, c);
+  API_END
+}
+
+int r2d3c_energy(r2d3c_ctx* ctx, const double* a, int kin, double* b) {
+  API_BEGIN
+  REQUIRE(ctx && a && b, "NULL argument");
+  ctx->eng->upload_spec(P_C1, a);
+  *b = energy_of(ctx->eng.get(), P_C1, kin);
+  API_END
+}
+
+int r2d3c_inerprod(r2d3c_ctx* ctx, const double* a, const double* b, int kin, double* rslt) {
+  API_BEGIN
+  REQUIRE(ctx && a && b && rslt, "NULL argument");
+  ctx->eng->upload_spec(P_C1, a);
+  ctx->eng->upload_spec(P_C2, b);
+  const int kind = 1, ia = 0, ib = 1;
+  const int pl[4] = {P_C1, P_C2, -1, -1};
+  ctx->eng->halfplane_sums(1, &kind, &ia, &ib, &kin, 0.0, 0.0, pl, rslt);
+  API_END
+}
+
+int r2d3c_dev_ptr(r2d3c_ctx* ctx, int which, void** ptr) {
+  API_BEGIN
+  REQUIRE(ctx && ptr, "NULL argument");
+  REQUIRE(which >= 0 && which <= 3, "which must be 0..3");
+  *ptr = ctx->eng->plane_ptr(which);
+  API_END
+}
+
+int r2d3c_stream(r2d3c_ctx* ctx, void** stream) {
+  API_BEGIN
+  REQUIRE(ctx && stream, "NULL argument");
+  *stream = (void*)ctx->eng->stream();
+  API_END
+}
+
+int r2d3c_synchronize(r2d3c_ctx* ctx) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  ctx->eng->sync();
+  API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,454 @@
+// Elementwise spectral operators, FP64 diagnostic reductions, forcing and
+// initial-condition kernels of the Rot2D3C hot path (sm_103a).
+#pragma once
+
+#include "r2d3c_kernels.cuh"
+
+namespace r2d3c {
+
+// ---------------------------------------------------------------------------
+// spectral elementwise operators (pseudospec2D_Rot2D3C.f90:6-127)
+// ---------------------------------------------------------------------------
+enum SpecOp : int {
+  OP_COPY_MASK = 0,   // derivk2 dir 0
+  OP_DERIV_X = 1,     // derivk2 dir 1: i*ka(i)*a, ka2 <= kmax
+  OP_DERIV_Y = 2,     // derivk2 dir 2: i*ka(j)*a, ka2 <= kmax
+  OP_LAPLA = 3,       // laplak2: -ka2*a
+  OP_INVLAPLA = 4,    // inv_laplak2: -a/ka2 where ka2 > tiny
+  OP_SCALE = 5,       // a*s          (field output, Rot2D3C.para.f90:476-491)
+  OP_SCALE_KA2 = 6,   // a*ka2*s      (vorticity output, :497-501)
+  OP_TRUNC_RECT = 7,  // zero outside the retained rectangle kx < M, |ky| <= L
+};
+
+// kx value of spectral column i (ka(i), Rot2D3C.para.f90:220-223)
+__device__ __forceinline__ int kx_of(int i, int n) { return i < (n >> 1) ? i : i - n; }
+
+template <typename T>
+__global__ void k_specop(const cpx<T>* __restrict__ a, cpx<T>* __restrict__ b, DevGrid gd, int op,
+                         double s) {
+  const size_t total = (size_t)gd.nh * gd.n;
+  const T sc = (T)s;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
+    const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
+    const int k2 = kx * kx + ky * ky;
+    const cpx<T> x = a[idx];
+    cpx<T> y;
+    switch (op) {
+      case OP_DERIV_X:
+        y = k2 <= gd.kmaxi ? mkc<T>(-(T)kx * x.y, (T)kx * x.x) : czero<T>();
+        break;
+      case OP_DERIV_Y:
+        y = k2 <= gd.kmaxi ? mkc<T>(-(T)ky * x.y, (T)ky * x.x) : czero<T>();
+        break;
+      case OP_LAPLA: {
+        const T m = -(T)k2;
+        y = mkc<T>(m * x.x, m * x.y);
+        break;
+      }
+      case OP_INVLAPLA:
+        y = k2 >= 1 ? mkc<T>(-x.x / (T)k2, -x.y / (T)k2) : czero<T>();
+        break;
+      case OP_SCALE:
+        y = mkc<T>(x.x * sc, x.y * sc);
+        break;
+      case OP_SCALE_KA2:
+        y = mkc<T>(x.x * (T)k2 * sc, x.y * (T)k2 * sc);
+        break;
+      case OP_TRUNC_RECT:
+        y = (i < gd.M && ky <= gd.L && -ky <= gd.L) ? x : czero<T>();
+        break;
+      default:  // OP_COPY_MASK
+        y = k2 <= gd.kmaxi ? x : czero<T>();
+        break;
+    }
+    b[idx] = y;
+  }
+}
+
+// r3 = r1*r2 (mode 0) or r3 = (r3 - r1*r2)*s (mode 1): poisson products
+// (pseudospec2D_Rot2D3C.f90:199-216); s = 1/n^4 is a power of two, so the
+// multiply equals the reference's division exactly.
+template <typename T>
+__global__ void k_realprod(T* __restrict__ r3, const T* __restrict__ r1, const T* __restrict__ r2,
+                           size_t count, int mode, double s) {
+  const T sc = (T)s;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const T p = r1[i] * r2[i];
+    r3[i] = mode == 0 ? p : (r3[i] - p) * sc;
+  }
+}
+
+template <typename Src, typename Dst>
+__global__ void k_convert(const Src* __restrict__ src, Dst* __restrict__ dst, size_t count) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;
+       i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (Dst)src[i];
+}
+
+// ---------------------------------------------------------------------------
+// half-plane sums (energy :336-396, inerprod :400-451, cond_check :455-568)
+// Every term sums two*w(k)*v over the half plane with two = 1 on the kx = 0
+// column; the 1/n^4 factor of the reference (a power of two) is applied once
+// to the total, which is exact.  Per-thread sequential sums, a fixed-shape
+// tree per CTA and a fixed-order pass over the CTA partials make every sum
+// reproducible run to run.
+// ---------------------------------------------------------------------------
+enum SumKind : int {
+  S_ENERGY = 0,      // |a|^2 ka2^kin; kin >= 0 all k, kin < 0 ka2 >= tiny
+  S_INERPROD = 1,    // ka2^kin Re(b conj a); ka2 <= kmax (kin >= 0), tiny <= ka2 <= kmax (kin < 0)
+  S_INERPROD_DY = 2, // inerprod(a, derivk2(b,2), 0)
+  S_BAND_KA2 = 3,    // ka2 |a|^2 for lo <= ka2 <= hi (energy in the kup band, :559-561)
+  S_BAND = 4,        // |a|^2 for lo <= ka2 <= hi
+};
+
+constexpr int kMaxTerms = 24;
+struct SumTerm {
+  int kind, ia, ib, kin;
+};
+struct SumList {
+  int nterms;
+  SumTerm t[kMaxTerms];
+  double band_lo, band_hi;
+};
+
+constexpr int kSumThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kSumThreads)
+k_halfplane_sums(const cpx<T>* __restrict__ p0, const cpx<T>* __restrict__ p1,
+                 const cpx<T>* __restrict__ p2, const cpx<T>* __restrict__ p3, DevGrid gd,
+                 SumList sl, double* __restrict__ partials) {
+  double acc[kMaxTerms];
+#pragma unroll
+  for (int t = 0; t < kMaxTerms; ++t) acc[t] = 0.0;
+  const cpx<T>* planes[4] = {p0, p1, p2, p3};
+  const size_t total = (size_t)gd.nh * gd.n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
+    const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
+    const int k2 = kx * kx + ky * ky;
+    const double ka2 = (double)k2;
+    const double two = i == 0 ? 1.0 : 2.0;
+    cpx<double> v[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      if (planes[p]) {
+        const cpx<T> x = planes[p][idx];
+        v[p] = mkc<double>((double)x.x, (double)x.y);
+      } else {
+        v[p] = mkc<double>(0.0, 0.0);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < kMaxTerms; ++t) {
+      if (t >= sl.nterms) break;
+      const SumTerm tm = sl.t[t];
+      const cpx<double> a = v[tm.ia], b = v[tm.ib];
+      double val = 0.0;
+      switch (tm.kind) {
+        case S_ENERGY:
+          if (tm.kin >= 0 || k2 >= 1) val = two * (a.x * a.x + a.y * a.y) * powi(ka2, tm.kin);
+          break;
+        case S_INERPROD:
+          if (k2 <= gd.kmaxi && (tm.kin >= 0 || k2 >= 1))
+            val = two * powi(ka2, tm.kin) * (b.x * a.x + b.y * a.y);
+          break;
+        case S_INERPROD_DY:
+          if (k2 <= gd.kmaxi) {
+            const double dx = -(double)ky * b.y, dy = (double)ky * b.x;
+            val = two * (dx * a.x + dy * a.y);
+          }
+          break;
+        case S_BAND_KA2:
+          if (ka2 <= sl.band_hi && ka2 >= sl.band_lo) val = two * ka2 * (a.x * a.x + a.y * a.y);
+          break;
+        default:  // S_BAND
+          if (ka2 <= sl.band_hi && ka2 >= sl.band_lo) val = two * (a.x * a.x + a.y * a.y);
+          break;
+      }
+      acc[t] += val;
+    }
+  }
+  __shared__ double red[kSumThreads];
+  for (int t = 0; t < sl.nterms; ++t) {
+    red[threadIdx.x] = acc[t];
+    __syncthreads();
+    for (int s = kSumThreads / 2; s > 0; s >>= 1) {
+      if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kMaxTerms + t] = red[0];
+    __syncthreads();
+  }
+}
+
+// out[t] = scale * sum_b partials[b][t], sequential over b (fixed order).
+static __global__ void k_finalize_sums(const double* __restrict__ partials, int nblocks, int nterms,
+                                double scale, double* __restrict__ out) {
+  const int t = threadIdx.x;
+  if (t >= nterms) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += partials[(size_t)b * kMaxTerms + t];
+  out[t] = s * scale;
+}
+
+// ---------------------------------------------------------------------------
+// shell sums (spectrum :615-712, transfers :715-837): one CTA per shell b,
+// kmn = int(sqrt(ka2)+.5) == b  <=>  (2b-1)^2 < 4 ka2 < (2b+1)^2.
+// out[(b-1)*5 + {0..4}] = Ek, Ezk, Fl0, Fl1, Fl2 (times 1/n^4).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long isqrt_ll(long long v) {
+  if (v <= 0) return 0;
+  long long r = (long long)sqrt((double)v);
+  while (r * r > v) --r;
+  while ((r + 1) * (r + 1) <= v) ++r;
+  return r;
+}
+
+constexpr int kShellThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kShellThreads)
+k_shells(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz,
+         const cpx<T>* __restrict__ c2, const cpx<T>* __restrict__ c1, DevGrid gd, double scale,
+         double* __restrict__ out) {
+  const int b = blockIdx.x + 1;
+  const int n = gd.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NW = kShellThreads / 32;
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  const long long lo = (long long)(2 * b - 1) * (2 * b - 1);
+  const long long hi = (long long)(2 * b + 1) * (2 * b + 1);
+  const int kxmax = min(b, n / 2);
+  for (int kx = warp; kx <= kxmax; kx += NW) {
+    const long long l2 = lo - 4LL * kx * kx;  // need 4 ky^2 > l2
+    const long long h2 = hi - 4LL * kx * kx;  // need 4 ky^2 < h2
+    if (h2 <= 0) continue;
+    long long kmin = 0;
+    if (l2 >= 0) {
+      kmin = isqrt_ll(l2 / 4);
+      while (4 * kmin * kmin <= l2) ++kmin;
+    }
+    long long kmaxk = isqrt_ll(h2 / 4) + 1;
+    while (kmaxk >= 0 && 4 * kmaxk * kmaxk >= h2) --kmaxk;
+    if (kmaxk < kmin) continue;
+    const double two = kx == 0 ? 1.0 : 2.0;
+    const double ka2c = (double)kx * kx;
+    // positive ky in [kmin, min(kmaxk, n/2-1)], negative ky in
+    // [-min(kmaxk, n/2), -max(kmin,1)]
+    for (int side = 0; side < 2; ++side) {
+      long long a0, a1;
+      if (side == 0) {
+        a0 = kmin;
+        a1 = min(kmaxk, (long long)(n / 2 - 1));
+      } else {
+        a0 = max(kmin, 1LL);
+        a1 = min(kmaxk, (long long)(n / 2));
+      }
+      for (long long k = a0 + lane; k <= a1; k += 32) {
+        const int j = side == 0 ? (int)k : (int)(n - k);
+        const size_t idx = (size_t)kx * n + j;
+        const double ka2 = ka2c + (double)(k * k);
+        const cpx<T> p = ps[idx], z = vz[idx];
+        const double pe = (double)p.x * p.x + (double)p.y * p.y;
+        acc[0] += two * ka2 * pe;
+        acc[1] += two * ((double)z.x * z.x + (double)z.y * z.y);
+        if (c2) {
+          const cpx<T> q2 = c2[idx], q1 = c1[idx];
+          const double r2 = (double)p.x * q2.x + (double)p.y * q2.y;
+          acc[2] += two * ka2 * r2;
+          acc[3] += two * r2;
+          acc[4] -= two * ((double)z.x * q1.x + (double)z.y * q1.y);
+        }
+      }
+    }
+  }
+  __shared__ double red[kShellThreads];
+  for (int t = 0; t < 5; ++t) {
+    red[threadIdx.x] = acc[t];
+    __syncthreads();
+    for (int s = kShellThreads / 2; s > 0; s >>= 1) {
+      if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(size_t)(b - 1) * 5 + t] = red[0] * scale;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CFL time step from the encoded max |grad psi|^2 (CFL_condition :892-895).
+// No FMA contraction, so the result equals the host FP64 formula bit for bit.
+// ---------------------------------------------------------------------------
+struct CflCoef {
+  double cfl, kcut, nrm, nuk, nuvk, w2;  // nuk = nu*kcut**(2nn), w2 = 2*omega
+};
+
+__device__ __forceinline__ double dec_ordered(unsigned long long e) {
+  const unsigned long long b = (e & 0x8000000000000000ULL) ? (e & 0x7fffffffffffffffULL) : ~e;
+  return __longlong_as_double((long long)b);
+}
+
+static __global__ void k_cfl_dt(const unsigned long long* __restrict__ enc, CflCoef c, double* scal,
+                         int add_time) {
+  const double m = dec_ordered(enc[0]);
+  const double tmp = __ddiv_rn(sqrt(m), c.nrm);
+  const double den = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(c.kcut, tmp), c.nuk), c.nuvk), c.w2);
+  const double dt = __ddiv_rn(c.cfl, den);
+  scal[0] = dt;
+  if (add_time) scal[1] = __dadd_rn(scal[1], dt);
+}
+
+static __global__ void k_add_time(double* scal) { scal[1] = __dadd_rn(scal[1], scal[0]); }
+
+// ---------------------------------------------------------------------------
+// rand_force (pseudospec2D_Rot2D3C.f90:1063-1126): the plane is zero except
+// at the chosen mode and, on the kx = 0 column, its conjugate mirror.  The
+// host draws the mode and phase; the amplitude sqrt(2 fp0)/(sqrt(dt) kup^kin)
+// is formed here from the device dt so a CFL step needs no host round trip.
+// ---------------------------------------------------------------------------
+struct RandForceField {
+  int nclear, clear[4];  // entries set by the previous call
+  int nset, set[4], conj[4];
+  double c0, kpow, cph, sph;  // sqrt(2 fp0), kup**kin, cos(phase), sin(phase)
+};
+struct RandForceArgs {
+  RandForceField f[2];
+  double nsq;  // dble(n)**2
+};
+
+template <typename T>
+__global__ void k_randforce(cpx<T>* fp, cpx<T>* fz, const double* __restrict__ scal, RandForceArgs a) {
+  const double dt = scal[0];
+  for (int fi = 0; fi < 2; ++fi) {
+    cpx<T>* dst = fi == 0 ? fp : fz;
+    const RandForceField& f = a.f[fi];
+    for (int c = 0; c < f.nclear; ++c) dst[f.clear[c]] = czero<T>();
+    const double tmp = __ddiv_rn(f.c0, __dmul_rn(sqrt(dt), f.kpow));
+    const double t1 = __dmul_rn(__dmul_rn(tmp, f.cph), a.nsq);
+    const double t2 = __dmul_rn(__dmul_rn(tmp, f.sph), a.nsq);
+    for (int c = 0; c < f.nset; ++c) dst[f.set[c]] = mkc<T>((T)t1, (T)(f.conj[c] ? -t2 : t2));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// physical-space initial condition (Rot2D3C.para.f90:255-279) and the
+// deterministic iflow = 1 forcing fields (:345-352)
+// ---------------------------------------------------------------------------
+struct IcMode {
+  double kr, ph1, ph2, ph3, ph4;
+  int ir, jr;
+};
+
+template <typename T>
+__global__ void k_ic_phys(const IcMode* __restrict__ modes, int nmodes, int n, double pi,
+                          T* __restrict__ r1, T* __restrict__ r2) {
+  const size_t total = (size_t)n * n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(idx / n), x = (int)(idx % n);
+    double a1 = 0.0, a2 = 0.0;
+    const double xi = (double)x, yj = (double)y, dn = (double)n;
+    for (int m = 0; m < nmodes; ++m) {
+      const IcMode md = modes[m];
+      const double ax = 2.0 * (md.ir - 1) * pi * xi / dn;
+      const double ay = 2.0 * (md.jr - 1) * pi * yj / dn;
+      a1 = a1 + cos(ax + md.ph1) * cos(ay + md.ph2) / md.kr;
+      a2 = a2 + sin(ax + md.ph3) * cos(ay + md.ph4);
+    }
+    r1[idx] = (T)a1;
+    r2[idx] = (T)a2;
+  }
+}
+
+template <typename T>
+__global__ void k_iflow1_phys(int n, double kup, double pi, T* __restrict__ r1, T* __restrict__ r2) {
+  const size_t total = (size_t)n * n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(idx / n), x = (int)(idx % n);
+    const double ax = 2 * kup * pi * (double)x / (double)n;
+    const double ay = 2 * kup * pi * (double)y / (double)n;
+    r1[idx] = (T)(sin(ax) + sin(ay));
+    r2[idx] = (T)(cos(ax) + sin(ay));
+  }
+}
+
+// Rescale inside the dealiasing mask tiny <= ka2 <= kmax, zero elsewhere
+// (Rot2D3C.para.f90:288-298 and :361-371).
+template <typename T>
+__global__ void k_scale_mask2(cpx<T>* a, cpx<T>* b, DevGrid gd, double sa, double sb) {
+  const size_t total = (size_t)gd.nh * gd.n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
+    const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
+    const int k2 = kx * kx + ky * ky;
+    const bool in = k2 <= gd.kmaxi && k2 >= 1;
+    const cpx<T> x = a[idx], y = b[idx];
+    a[idx] = in ? mkc<T>((T)(sa * (double)x.x), (T)(sa * (double)x.y)) : czero<T>();
+    b[idx] = in ? mkc<T>((T)(sb * (double)y.x), (T)(sb * (double)y.y)) : czero<T>();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// const_inj (pseudospec2D_Rot2D3C.f90:977-1060), iflow = 2.  The reference
+// reseeds randu with myrank before the rescaling loop (:1032), so the random
+// factors of the band elements form one fixed sequence in loop order; the
+// host precomputes it together with the band element list.
+// ---------------------------------------------------------------------------
+// fp = ps/(|ps|^2+1) in kdn^2 <= ka2 <= kup^2, Hermitian fill on kx = 0
+// (:1005-1028)
+template <typename T>
+__global__ void k_ci_base(const cpx<T>* __restrict__ src, cpx<T>* __restrict__ dst, DevGrid gd,
+                          double lo, double hi) {
+  const size_t total = (size_t)gd.nh * gd.n;
+  const int n = gd.n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / n), j = (int)(idx % n);
+    const int kx = kx_of(i, n), ky = ky_of(j, n);
+    const double ka2 = (double)(kx * kx + ky * ky);
+    const bool band = ka2 <= hi && ka2 >= lo;
+    cpx<T> out = czero<T>();
+    if (i != 0) {
+      if (band) {
+        const cpx<T> p = src[idx];
+        const double d = (double)p.x * p.x + (double)p.y * p.y + 1.0;
+        out = mkc<T>((T)((double)p.x / d), (T)((double)p.y / d));
+      }
+    } else if (j != 0 && j != n / 2 && band) {
+      const int js = j < n / 2 ? j : n - j;
+      const cpx<T> p = src[js];
+      const double d = (double)p.x * p.x + (double)p.y * p.y + 1.0;
+      out = mkc<T>((T)((double)p.x / d), (T)(j < n / 2 ? (double)p.y / d : -((double)p.y / d)));
+    }
+    dst[idx] = out;
+  }
+}
+
+// fp = fp*fp0/Efp + i*randu*|k|*ps on the band (:1033-1057)
+template <typename T>
+__global__ void k_ci_rescale(const cpx<T>* __restrict__ src, cpx<T>* __restrict__ dst,
+                             const int* __restrict__ band_idx, const int* __restrict__ mirror,
+                             const float* __restrict__ rnd, int nband, double f0,
+                             const double* __restrict__ efp, int n) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nband) return;
+  const int idx = band_idx[e];
+  const int i = idx / n, j = idx % n;
+  const int kx = kx_of(i, n), ky = ky_of(j, n);
+  const double t3 = (double)rnd[e] * sqrt((double)(kx * kx + ky * ky));
+  const double E = *efp;
+  const cpx<T> f = dst[idx], p = src[idx];
+  const double vx = ((double)f.x * f0) / E + (-t3 * (double)p.y);
+  const double vy = ((double)f.y * f0) / E + (t3 * (double)p.x);
+  dst[idx] = mkc<T>((T)vx, (T)vy);
+  if (mirror[e] >= 0) dst[mirror[e]] = mkc<T>((T)vx, (T)(-vy));
+}
+
+}  // namespace r2d3c

@@ -1,0 +1,116 @@
+// Precision-independent interface between the C-ABI layer and the device
+// engine of one context (FP64 or FP32 compute type).  All planes live in
+// device memory owned by the engine; all work is queued on the engine's
+// stream.  Methods throw r2d3c::Error on CUDA failures; the C-ABI layer turns
+// them into status codes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace r2d3c {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// status codes mirrored from include/r2d3c.h
+constexpr int kOK = 0, kEINVAL = -1, kECUDA = -2, kENOMEM = -3, kETIMEOUT = -4, kEIO = -5,
+              kESTATE = -6;
+
+void cuda_check(cudaError_t e, const char* what);
+
+// Spectral planes: complex [kx][ky], (n/2+1) x n.
+enum Plane : int { P_PS = 0, P_VZ, P_FP, P_FZ, P_C1, P_C2, P_W1, P_W2, P_B5, P_B6, P_COUNT };
+// Real planes: [y][x], n x n.
+enum RPlane : int { R_1 = 0, R_2, R_3, R_COUNT };
+
+struct ModelCoef {
+  double nu, hnu, nuv, hnuv, omega;
+  int nn, mm, nnv, mmv;
+};
+
+struct RandForceHost {  // one field of one rand_force call
+  int nset;
+  int set[4];
+  int conj[4];
+  double c0, kpow, cph, sph;
+};
+
+struct IcModeHost {
+  double kr, ph1, ph2, ph3, ph4;
+  int ir, jr;
+};
+
+class IEngine {
+ public:
+  virtual ~IEngine() {}
+  virtual int n() const = 0;
+  virtual int precision() const = 0;  // 0 = FP64, 1 = FP32
+  virtual cudaStream_t stream() const = 0;
+  virtual void* plane_ptr(int plane) = 0;
+  virtual void* rplane_ptr(int rplane) = 0;
+  virtual size_t bytes_allocated() const = 0;
+
+  // host <-> device (FP64 host arrays, synchronous on return)
+  virtual void upload_spec(int plane, const double* host) = 0;    // 2*(n/2+1)*n doubles
+  virtual void download_spec(int plane, double* host) = 0;
+  virtual void upload_real(int rplane, const double* host) = 0;   // n*n doubles
+  virtual void download_real(int rplane, double* host) = 0;
+  // device FP64 <-> planes (for callers that keep data on the GPU)
+  virtual void spec_from_dev64(int plane, const double* dev) = 0;
+  virtual void spec_to_dev64(int plane, double* dev) = 0;
+  virtual void real_from_dev64(int rplane, const double* dev) = 0;
+  virtual void real_to_dev64(int rplane, double* dev) = 0;
+
+  // generic operators
+  virtual void specop(int src, int dst, int op, double s) = 0;
+  virtual void zero_spec(int plane) = 0;
+  virtual void r2c(int rsrc, int dst) = 0;
+  virtual void c2r(int src, int rdst, double* mx, double* mn) = 0;  // rdst<0: no store
+  virtual void poisson(int a, int b, int c) = 0;
+  virtual void halfplane_sums(int nterms, const int* kind, const int* ia, const int* ib,
+                              const int* kin, double band_lo, double band_hi, const int* planes4,
+                              double* out) = 0;
+  virtual void shells(bool transfers, double* out5) = 0;  // (n/2+1) x 5
+  virtual double cfl(double cfl, const ModelCoef& mc) = 0;
+
+  // hot path
+  virtual void set_dt(double dt) = 0;
+  virtual void set_time(double t) = 0;
+  virtual double get_dt() = 0;
+  virtual double get_time() = 0;
+  virtual void mark_state_untruncated() = 0;
+  virtual void rand_force(const RandForceHost f[2]) = 0;
+  // One RK4 step.  cfl_mode: dt from the CFL condition of the current state
+  // (fused into the first substep), else the dt already set.  add_time:
+  // time += dt on the device.  rf: per-step forcing draws (iflow = 3) or null.
+  virtual void step(const ModelCoef& mc, bool cfl_mode, double cfl, bool add_time,
+                    const RandForceHost* rf) = 0;
+  // nsteps steps replayed from one captured CUDA graph; rf holds 2*nsteps
+  // forcing draws (iflow = 3) or is null.
+  virtual void advance(const ModelCoef& mc, int nsteps, bool cfl_mode, double cfl,
+                       const RandForceHost* rf) = 0;
+  virtual void initial_condition_phys(const std::vector<IcModeHost>& modes) = 0;  // -> R_1, R_2
+  virtual void iflow1_phys(double kup) = 0;                                        // -> R_1, R_2
+  virtual void scale_mask2(int a, int b, double sa, double sb) = 0;
+  // const_inj (iflow = 2): configure the band (loop-order element list, kx=0
+  // mirrors, random factors); when enabled every RK substep rebuilds fp, fz.
+  virtual void set_const_inj(bool on, double kdn, double kup, double fp0, double fz0,
+                             const std::vector<int>& band_idx, const std::vector<int>& mirror,
+                             const std::vector<float>& rnd) = 0;
+  virtual void const_inj(int src, int dst, int kin, double f0) = 0;
+  virtual void sync() = 0;
+  virtual int kernel_launches() const = 0;
+};
+
+// full = false allocates only what the Level-1 transforms need.
+IEngine* make_engine_f64(int n, int device, bool full);
+IEngine* make_engine_f32(int n, int device, bool full);
+bool supported_n(int n);
+
+}  // namespace r2d3c

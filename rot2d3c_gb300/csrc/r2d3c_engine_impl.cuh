@@ -1,0 +1,758 @@
+// Device engine of one Rot2D3C context, templated on the compute type
+// (double: the FP64 drop-in path; float: the FP32 path with compensated
+// twiddles and FP64 reductions).  Included by one translation unit per type.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "r2d3c_aux.cuh"
+#include "r2d3c_engine.h"
+
+namespace r2d3c {
+
+template <typename F>
+void dispatch_n(int n, F&& f) {
+  switch (n) {
+    case 16: f(std::integral_constant<int, 16>{}); break;
+    case 32: f(std::integral_constant<int, 32>{}); break;
+    case 64: f(std::integral_constant<int, 64>{}); break;
+    case 128: f(std::integral_constant<int, 128>{}); break;
+    case 256: f(std::integral_constant<int, 256>{}); break;
+    case 512: f(std::integral_constant<int, 512>{}); break;
+    case 1024: f(std::integral_constant<int, 1024>{}); break;
+    case 2048: f(std::integral_constant<int, 2048>{}); break;
+    case 4096: f(std::integral_constant<int, 4096>{}); break;
+    case 8192: f(std::integral_constant<int, 8192>{}); break;
+    default: throw Error(kEINVAL, "unsupported grid size n");
+  }
+}
+
+template <typename K>
+inline void set_smem_attr(K kernel, size_t smem) {
+  if (smem > 48 * 1024)
+    cuda_check(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "cudaFuncSetAttribute(max dynamic smem)");
+}
+
+// max over x of r1^2 + r2^2 (CFL_condition :867-874), encoded for atomicMax
+template <typename T>
+__global__ void k_max_sq2(const T* __restrict__ r1, const T* __restrict__ r2, size_t count,
+                          unsigned long long* enc) {
+  double m = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double a = (double)r1[i], b = (double)r2[i];
+    m = fmax(m, a * a + b * b);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(enc, enc_ordered(m));
+}
+
+// rand_force for step *ctr of a precomputed sequence (graph replay)
+template <typename T>
+__global__ void k_randforce_seq(cpx<T>* fp, cpx<T>* fz, const double* __restrict__ scal,
+                                const RandForceArgs* __restrict__ seq, int* ctr) {
+  const int s = *ctr;
+  const RandForceArgs a = seq[s];
+  const double dt = scal[0];
+  for (int fi = 0; fi < 2; ++fi) {
+    cpx<T>* dst = fi == 0 ? fp : fz;
+    const RandForceField& f = a.f[fi];
+    for (int c = 0; c < f.nclear; ++c) dst[f.clear[c]] = czero<T>();
+    const double tmp = __ddiv_rn(f.c0, __dmul_rn(sqrt(dt), f.kpow));
+    const double t1 = __dmul_rn(__dmul_rn(tmp, f.cph), a.nsq);
+    const double t2 = __dmul_rn(__dmul_rn(tmp, f.sph), a.nsq);
+    for (int c = 0; c < f.nset; ++c) dst[f.set[c]] = mkc<T>((T)t1, (T)(f.conj[c] ? -t2 : t2));
+  }
+  *ctr = s + 1;
+}
+
+template <typename T>
+class EngineT final : public IEngine {
+ public:
+  EngineT(int n, int device, bool full) : n_(n), dev_(device), full_(full) {
+    if (!supported_n(n)) throw Error(kEINVAL, "unsupported grid size n");
+    cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    cuda_check(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking), "cudaStreamCreate");
+    gd_.n = n;
+    gd_.nh = n / 2 + 1;
+    const double kmax = ((double)n / 3.0) * ((double)n / 3.0);  // (n/3)**2
+    gd_.kmaxi = (int)std::floor(kmax);
+    gd_.L = (int)std::floor((double)n / 3.0);
+    gd_.M = gd_.L + 1;
+    S_ = (size_t)gd_.nh * n;
+    try {
+      for (int p = 0; p < P_COUNT; ++p)
+        if (full || p == P_W1) planes_[p] = alloc<cpx<T>>(S_);
+      for (int r = 0; r < R_COUNT; ++r)
+        if (full || r == R_1) rplanes_[r] = alloc<T>((size_t)n * n);
+      if (full) {
+        tf_ = alloc<cpx<T>>((size_t)6 * gd_.M * n);
+        pb_ = alloc<cpx<T>>(2 * S_);
+      }
+      tg_ = alloc<cpx<T>>(S_);
+      tw_ = alloc<tw_t<T>>((size_t)n);
+      stage_count_ = std::max(2 * S_, (size_t)n * n);
+      if (!std::is_same<T, double>::value) stage64_ = alloc<double>(stage_count_);
+      scal_ = alloc<double>(8);
+      enc_ = alloc<unsigned long long>(8);
+      partials_ = alloc<double>((size_t)kSumBlocks * kMaxTerms);
+      small_ = alloc<double>((size_t)kMaxTerms + 5 * (size_t)gd_.nh);
+      cuda_check(cudaMallocHost(&hsmall_, sizeof(double) * (kMaxTerms + 5 * (size_t)gd_.nh + 16)),
+                 "cudaMallocHost");
+      cuda_check(cudaMemsetAsync(scal_, 0, 8 * sizeof(double), st_), "memset");
+      for (int p = 0; p < P_COUNT; ++p)
+        if (planes_[p]) zero_spec(p);
+      build_twiddles();
+      set_kernel_attrs();
+      sync();
+    } catch (...) {
+      release();
+      throw;
+    }
+  }
+  ~EngineT() override { release(); }
+
+  int n() const override { return n_; }
+  int precision() const override { return std::is_same<T, double>::value ? 0 : 1; }
+  cudaStream_t stream() const override { return st_; }
+  void* plane_ptr(int p) override { return planes_[p]; }
+  void* rplane_ptr(int r) override { return rplanes_[r]; }
+  size_t bytes_allocated() const override { return bytes_; }
+  int kernel_launches() const override { return launches_; }
+
+  // ---------------------------------------------------------------- transfers
+  void upload_spec(int p, const double* host) override {
+    if (std::is_same<T, double>::value) {
+      cuda_check(cudaMemcpyAsync(planes_[p], host, S_ * 2 * sizeof(double), cudaMemcpyHostToDevice, st_),
+                 "H2D spec");
+    } else {
+      cuda_check(cudaMemcpyAsync(stage64_, host, S_ * 2 * sizeof(double), cudaMemcpyHostToDevice, st_),
+                 "H2D spec");
+      convert(stage64_, reinterpret_cast<T*>(planes_[p]), 2 * S_);
+    }
+    sync();
+  }
+  void download_spec(int p, double* host) override {
+    if (std::is_same<T, double>::value) {
+      cuda_check(cudaMemcpyAsync(host, planes_[p], S_ * 2 * sizeof(double), cudaMemcpyDeviceToHost, st_),
+                 "D2H spec");
+    } else {
+      convert(reinterpret_cast<const T*>(planes_[p]), stage64_, 2 * S_);
+      cuda_check(cudaMemcpyAsync(host, stage64_, S_ * 2 * sizeof(double), cudaMemcpyDeviceToHost, st_),
+                 "D2H spec");
+    }
+    sync();
+  }
+  void upload_real(int r, const double* host) override {
+    const size_t cnt = (size_t)n_ * n_;
+    if (std::is_same<T, double>::value) {
+      cuda_check(cudaMemcpyAsync(rplanes_[r], host, cnt * sizeof(double), cudaMemcpyHostToDevice, st_), "H2D real");
+    } else {
+      cuda_check(cudaMemcpyAsync(stage64_, host, cnt * sizeof(double), cudaMemcpyHostToDevice, st_), "H2D real");
+      convert(stage64_, rplanes_[r], cnt);
+    }
+    sync();
+  }
+  void download_real(int r, double* host) override {
+    const size_t cnt = (size_t)n_ * n_;
+    if (std::is_same<T, double>::value) {
+      cuda_check(cudaMemcpyAsync(host, rplanes_[r], cnt * sizeof(double), cudaMemcpyDeviceToHost, st_), "D2H real");
+    } else {
+      convert(rplanes_[r], stage64_, cnt);
+      cuda_check(cudaMemcpyAsync(host, stage64_, cnt * sizeof(double), cudaMemcpyDeviceToHost, st_), "D2H real");
+    }
+    sync();
+  }
+  void spec_from_dev64(int p, const double* dev) override {
+    if (std::is_same<T, double>::value)
+      cuda_check(cudaMemcpyAsync(planes_[p], dev, S_ * 2 * sizeof(double), cudaMemcpyDeviceToDevice, st_), "D2D");
+    else
+      convert(dev, reinterpret_cast<T*>(planes_[p]), 2 * S_);
+  }
+  void spec_to_dev64(int p, double* dev) override {
+    if (std::is_same<T, double>::value)
+      cuda_check(cudaMemcpyAsync(dev, planes_[p], S_ * 2 * sizeof(double), cudaMemcpyDeviceToDevice, st_), "D2D");
+    else
+      convert(reinterpret_cast<const T*>(planes_[p]), dev, 2 * S_);
+  }
+  void real_from_dev64(int r, const double* dev) override {
+    const size_t cnt = (size_t)n_ * n_;
+    if (std::is_same<T, double>::value)
+      cuda_check(cudaMemcpyAsync(rplanes_[r], dev, cnt * sizeof(double), cudaMemcpyDeviceToDevice, st_), "D2D");
+    else
+      convert(dev, rplanes_[r], cnt);
+  }
+  void real_to_dev64(int r, double* dev) override {
+    const size_t cnt = (size_t)n_ * n_;
+    if (std::is_same<T, double>::value)
+      cuda_check(cudaMemcpyAsync(dev, rplanes_[r], cnt * sizeof(double), cudaMemcpyDeviceToDevice, st_), "D2D");
+    else
+      convert(rplanes_[r], dev, cnt);
+  }
+
+  // ---------------------------------------------------------------- operators
+  void specop(int src, int dst, int op, double s) override {
+    k_specop<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[src], planes_[dst], gd_, op, s);
+    post("k_specop");
+  }
+  void zero_spec(int p) override {
+    cuda_check(cudaMemsetAsync(planes_[p], 0, S_ * sizeof(cpx<T>), st_), "memset plane");
+  }
+  void r2c(int rsrc, int dst) override {
+    launch_rowr2c(rplanes_[rsrc], tg_);
+    launch_colfft<-1>(tg_, planes_[dst], gd_.nh);
+  }
+  void c2r(int src, int rdst, double* mx, double* mn) override {
+    launch_colfft<+1>(planes_[src], tg_, gd_.nh);
+    if (mx) cuda_check(cudaMemsetAsync(enc_ + 1, 0, 2 * sizeof(unsigned long long), st_), "memset");
+    launch_rowc2r(tg_, rdst >= 0 ? rplanes_[rdst] : nullptr, mx ? enc_ + 1 : nullptr);
+    if (mx) {
+      unsigned long long e[2];
+      cuda_check(cudaMemcpyAsync(e, enc_ + 1, sizeof(e), cudaMemcpyDeviceToHost, st_), "D2H minmax");
+      sync();
+      *mx = dec_host(e[0]);
+      *mn = -dec_host(e[1]);
+    }
+  }
+  void poisson(int a, int b, int c) override {
+    const size_t cnt = (size_t)n_ * n_;
+    const double inv4 = 1.0 / ((double)n_ * n_ * n_ * n_);
+    specop(a, P_W1, OP_DERIV_X, 0.0);
+    specop(b, P_W2, OP_DERIV_Y, 0.0);
+    c2r(P_W1, R_1, nullptr, nullptr);
+    c2r(P_W2, R_2, nullptr, nullptr);
+    k_realprod<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_3], rplanes_[R_1], rplanes_[R_2], cnt, 0, 1.0);
+    post("k_realprod");
+    specop(a, P_W1, OP_DERIV_Y, 0.0);
+    specop(b, P_W2, OP_DERIV_X, 0.0);
+    c2r(P_W1, R_1, nullptr, nullptr);
+    c2r(P_W2, R_2, nullptr, nullptr);
+    k_realprod<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_3], rplanes_[R_1], rplanes_[R_2], cnt, 1, inv4);
+    post("k_realprod");
+    r2c(R_3, c);
+  }
+  void halfplane_sums(int nterms, const int* kind, const int* ia, const int* ib, const int* kin,
+                      double band_lo, double band_hi, const int* planes4, double* out) override {
+    enqueue_sums(nterms, kind, ia, ib, kin, band_lo, band_hi, planes4);
+    cuda_check(cudaMemcpyAsync(hsmall_, small_, nterms * sizeof(double), cudaMemcpyDeviceToHost, st_), "D2H sums");
+    sync();
+    std::memcpy(out, hsmall_, nterms * sizeof(double));
+  }
+  // sums into small_[0..nterms) on the device
+  void enqueue_sums(int nterms, const int* kind, const int* ia, const int* ib, const int* kin,
+                    double band_lo, double band_hi, const int* planes4) {
+    if (nterms < 1 || nterms > kMaxTerms) throw Error(kEINVAL, "bad number of sum terms");
+    SumList sl;
+    std::memset(&sl, 0, sizeof(sl));
+    sl.nterms = nterms;
+    for (int t = 0; t < nterms; ++t) sl.t[t] = SumTerm{kind[t], ia[t], ib[t], kin[t]};
+    sl.band_lo = band_lo;
+    sl.band_hi = band_hi;
+    const cpx<T>* p[4];
+    for (int i = 0; i < 4; ++i) p[i] = planes4[i] >= 0 ? planes_[planes4[i]] : nullptr;
+    k_halfplane_sums<T><<<kSumBlocks, kSumThreads, 0, st_>>>(p[0], p[1], p[2], p[3], gd_, sl, partials_);
+    post("k_halfplane_sums");
+    const double inv4 = 1.0 / ((double)n_ * n_ * n_ * n_);
+    k_finalize_sums<<<1, 32, 0, st_>>>(partials_, kSumBlocks, nterms, inv4, small_);
+    post("k_finalize_sums");
+  }
+
+  void set_const_inj(bool on, double kdn, double kup, double fp0, double fz0,
+                     const std::vector<int>& band_idx, const std::vector<int>& mirror,
+                     const std::vector<float>& rnd) override {
+    ci_on_ = false;
+    for (void* p : {(void*)ci_idx_, (void*)ci_mir_, (void*)ci_rnd_})
+      if (p) cudaFree(p);
+    ci_idx_ = nullptr;
+    ci_mir_ = nullptr;
+    ci_rnd_ = nullptr;
+    ci_n_ = (int)band_idx.size();
+    ci_lo_ = kdn * kdn;
+    ci_hi_ = kup * kup;
+    ci_fp0_ = fp0;
+    ci_fz0_ = fz0;
+    const size_t c = std::max<size_t>(band_idx.size(), 1);
+    cuda_check(cudaMalloc(&ci_idx_, c * sizeof(int)), "cudaMalloc band");
+    cuda_check(cudaMalloc(&ci_mir_, c * sizeof(int)), "cudaMalloc band");
+    cuda_check(cudaMalloc(&ci_rnd_, c * sizeof(float)), "cudaMalloc band");
+    if (ci_n_ > 0) {
+      cuda_check(cudaMemcpyAsync(ci_idx_, band_idx.data(), ci_n_ * sizeof(int), cudaMemcpyHostToDevice, st_), "H2D");
+      cuda_check(cudaMemcpyAsync(ci_mir_, mirror.data(), ci_n_ * sizeof(int), cudaMemcpyHostToDevice, st_), "H2D");
+      cuda_check(cudaMemcpyAsync(ci_rnd_, rnd.data(), ci_n_ * sizeof(float), cudaMemcpyHostToDevice, st_), "H2D");
+    }
+    sync();
+    ci_on_ = on;
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+  }
+  void const_inj(int src, int dst, int kin, double f0) override {
+    if (!ci_idx_) throw Error(kESTATE, "const_inj band not configured");
+    enqueue_const_inj(planes_[src], src, dst, kin, f0);
+  }
+  void enqueue_const_inj(const cpx<T>* srcp, int src_slot_plane, int dst, int kin, double f0) {
+    k_ci_base<T><<<elem_blocks(S_), 256, 0, st_>>>(srcp, planes_[dst], gd_, ci_lo_, ci_hi_);
+    post("k_ci_base");
+    // Efp = inerprod(ps, fp, kin) (:1030), kept on the device
+    const int kind = S_INERPROD, ia = 0, ib = 1;
+    const int pl[4] = {src_slot_plane, dst, -1, -1};
+    enqueue_sums(1, &kind, &ia, &ib, &kin, 0.0, 0.0, pl);
+    if (ci_n_ > 0) {
+      k_ci_rescale<T><<<(ci_n_ + 255) / 256, 256, 0, st_>>>(srcp, planes_[dst], ci_idx_, ci_mir_, ci_rnd_,
+                                                            ci_n_, f0, small_, n_);
+      post("k_ci_rescale");
+    }
+  }
+  void brackets_full() {
+    // [psi, -k^2 psi] -> B5 and [psi, vz] -> B6 over the whole half plane
+    launch_passA(planes_[P_PS], planes_[P_VZ]);
+    launch_passB<false>(gd_.nh);
+    launch_colfft<-1>(pb_, planes_[P_B5], gd_.nh);
+    launch_colfft<-1>(pb_ + S_, planes_[P_B6], gd_.nh);
+  }
+  void shells(bool transfers, double* out5) override {
+    if (transfers) brackets_full();
+    const double inv4 = 1.0 / ((double)n_ * n_ * n_ * n_);
+    double* dout = small_ + kMaxTerms;
+    k_shells<T><<<gd_.nh, kShellThreads, 0, st_>>>(planes_[P_PS], planes_[P_VZ],
+                                                    transfers ? planes_[P_B5] : nullptr,
+                                                    transfers ? planes_[P_B6] : nullptr, gd_, inv4, dout);
+    post("k_shells");
+    cuda_check(cudaMemcpyAsync(hsmall_, dout, 5 * (size_t)gd_.nh * sizeof(double), cudaMemcpyDeviceToHost, st_),
+               "D2H shells");
+    sync();
+    std::memcpy(out5, hsmall_, 5 * (size_t)gd_.nh * sizeof(double));
+  }
+  CflCoef cfl_coef(double cfl, const ModelCoef& mc) const {
+    CflCoef c;
+    c.cfl = cfl;
+    c.kcut = (double)n_ / 3.0;
+    c.nrm = (double)n_ * (double)n_;
+    c.nuk = mc.nu * ipow(c.kcut, 2 * mc.nn);
+    c.nuvk = mc.nuv * ipow(c.kcut, 2 * mc.nnv);
+    c.w2 = 2 * mc.omega;
+    return c;
+  }
+  double cfl(double cfl, const ModelCoef& mc) override {
+    const size_t cnt = (size_t)n_ * n_;
+    specop(P_PS, P_W1, OP_DERIV_X, 0.0);
+    specop(P_PS, P_W2, OP_DERIV_Y, 0.0);
+    c2r(P_W1, R_1, nullptr, nullptr);
+    c2r(P_W2, R_2, nullptr, nullptr);
+    cuda_check(cudaMemsetAsync(enc_, 0, sizeof(unsigned long long), st_), "memset");
+    k_max_sq2<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_1], rplanes_[R_2], cnt, enc_);
+    post("k_max_sq2");
+    k_cfl_dt<<<1, 1, 0, st_>>>(enc_, cfl_coef(cfl, mc), scal_, 0);
+    post("k_cfl_dt");
+    return get_dt();
+  }
+
+  // ---------------------------------------------------------------- hot path
+  void set_dt(double dt) override { set_scal(0, dt); }
+  void set_time(double t) override { set_scal(1, t); }
+  double get_dt() override { return get_scal(0); }
+  double get_time() override { return get_scal(1); }
+  void mark_state_untruncated() override { dirty_ = true; }
+
+  void rand_force(const RandForceHost f[2]) override {
+    RandForceArgs a = make_rf_args(f);
+    k_randforce<T><<<1, 1, 0, st_>>>(planes_[P_FP], planes_[P_FZ], scal_, a);
+    post("k_randforce");
+  }
+
+  void step(const ModelCoef& mc, bool cfl_mode, double cfl, bool add_time,
+            const RandForceHost* rf) override {
+    truncate_if_dirty();
+    enqueue_step(mc, cfl_mode, cfl, add_time, rf ? 1 : 0, rf);
+  }
+
+  void advance(const ModelCoef& mc, int nsteps, bool cfl_mode, double cfl,
+               const RandForceHost* rf) override {
+    if (nsteps <= 0) return;
+    truncate_if_dirty();
+    if (rf) {
+      if (rf_cap_ < nsteps) {
+        if (d_rf_) cudaFree(d_rf_);
+        d_rf_ = nullptr;
+        rf_cap_ = 0;
+        cuda_check(cudaMalloc(&d_rf_, sizeof(RandForceArgs) * (size_t)nsteps), "cudaMalloc rf");
+        rf_cap_ = nsteps;
+        if (!d_ctr_) cuda_check(cudaMalloc(&d_ctr_, sizeof(int)), "cudaMalloc ctr");
+      }
+      std::vector<RandForceArgs> seq((size_t)nsteps);
+      for (int s = 0; s < nsteps; ++s) seq[s] = make_rf_args(rf + 2 * s);
+      cuda_check(cudaMemcpyAsync(d_rf_, seq.data(), sizeof(RandForceArgs) * (size_t)nsteps,
+                                 cudaMemcpyHostToDevice, st_), "H2D rf");
+      cuda_check(cudaMemsetAsync(d_ctr_, 0, sizeof(int), st_), "memset ctr");
+      sync();  // seq goes out of scope
+    }
+    GraphKey key{cfl_mode, rf != nullptr, cfl, mc};
+    if (!graph_ || !key.same(gkey_)) {
+      if (graph_) cudaGraphExecDestroy(graph_);
+      graph_ = nullptr;
+      cudaGraph_t g;
+      const int before = launches_;
+      cuda_check(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal), "BeginCapture");
+      try {
+        enqueue_step(mc, cfl_mode, cfl, true, rf ? -1 : 0, nullptr);
+      } catch (...) {
+        cudaStreamEndCapture(st_, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      cuda_check(cudaStreamEndCapture(st_, &g), "EndCapture");
+      cuda_check(cudaGraphInstantiate(&graph_, g, 0), "GraphInstantiate");
+      cudaGraphDestroy(g);
+      graph_launches_ = launches_ - before;
+      launches_ = before;
+      gkey_ = key;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+      cuda_check(cudaGraphLaunch(graph_, st_), "GraphLaunch");
+      launches_ += graph_launches_;
+    }
+  }
+
+  void initial_condition_phys(const std::vector<IcModeHost>& modes) override {
+    IcMode* d = nullptr;
+    const size_t bytes = sizeof(IcMode) * std::max<size_t>(modes.size(), 1);
+    cuda_check(cudaMalloc(&d, bytes), "cudaMalloc ic modes");
+    std::vector<IcMode> hm(modes.size());
+    for (size_t i = 0; i < modes.size(); ++i)
+      hm[i] = IcMode{modes[i].kr, modes[i].ph1, modes[i].ph2, modes[i].ph3, modes[i].ph4, modes[i].ir, modes[i].jr};
+    try {
+      if (!hm.empty())
+        cuda_check(cudaMemcpyAsync(d, hm.data(), sizeof(IcMode) * hm.size(), cudaMemcpyHostToDevice, st_), "H2D ic");
+      k_ic_phys<T><<<elem_blocks((size_t)n_ * n_), 256, 0, st_>>>(d, (int)hm.size(), n_, kPi,
+                                                                   rplanes_[R_1], rplanes_[R_2]);
+      post("k_ic_phys");
+      sync();
+    } catch (...) {
+      cudaFree(d);
+      throw;
+    }
+    cudaFree(d);
+  }
+  void iflow1_phys(double kup) override {
+    k_iflow1_phys<T><<<elem_blocks((size_t)n_ * n_), 256, 0, st_>>>(n_, kup, kPi, rplanes_[R_1], rplanes_[R_2]);
+    post("k_iflow1_phys");
+  }
+  void scale_mask2(int a, int b, double sa, double sb) override {
+    k_scale_mask2<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[a], planes_[b], gd_, sa, sb);
+    post("k_scale_mask2");
+  }
+  void sync() override { cuda_check(cudaStreamSynchronize(st_), "cudaStreamSynchronize"); }
+
+ private:
+  static constexpr int kSumBlocks = 304;  // 2 CTAs per SM on 152 SMs
+  static constexpr double kPi = 3.1415926535897932384;
+
+  struct GraphKey {
+    bool cfl_mode = false, rf = false;
+    double cfl = 0.0;
+    ModelCoef mc{};
+    bool same(const GraphKey& o) const {
+      return cfl_mode == o.cfl_mode && rf == o.rf && cfl == o.cfl &&
+             std::memcmp(&mc, &o.mc, sizeof(ModelCoef)) == 0;
+    }
+  };
+
+  template <typename U>
+  U* alloc(size_t count) {
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, count * sizeof(U));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(kENOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    owned_.push_back(p);
+    bytes_ += count * sizeof(U);
+    return reinterpret_cast<U*>(p);
+  }
+  void release() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+    for (void* p : owned_) cudaFree(p);
+    owned_.clear();
+    if (d_rf_) cudaFree(d_rf_);
+    if (d_ctr_) cudaFree(d_ctr_);
+    for (void* p : {(void*)ci_idx_, (void*)ci_mir_, (void*)ci_rnd_})
+      if (p) cudaFree(p);
+    ci_idx_ = nullptr;
+    ci_mir_ = nullptr;
+    ci_rnd_ = nullptr;
+    d_rf_ = nullptr;
+    d_ctr_ = nullptr;
+    if (hsmall_) cudaFreeHost(hsmall_);
+    hsmall_ = nullptr;
+    if (st_) cudaStreamDestroy(st_);
+    st_ = nullptr;
+  }
+  static unsigned elem_blocks(size_t count) {
+    const size_t b = (count + 255) / 256;
+    return (unsigned)std::min<size_t>(b, 152 * 16);
+  }
+  void post(const char* what) {
+    ++launches_;
+    cuda_check(cudaGetLastError(), what);
+  }
+  template <typename S, typename D>
+  void convert(const S* src, D* dst, size_t count) {
+    k_convert<S, D><<<elem_blocks(count), 256, 0, st_>>>(src, dst, count);
+    post("k_convert");
+  }
+  static double dec_host(unsigned long long e) {
+    const unsigned long long b = (e & 0x8000000000000000ULL) ? (e & 0x7fffffffffffffffULL) : ~e;
+    double d;
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+  }
+  static double ipow(double x, int k) {  // REAL**INTEGER by repeated squaring
+    if (k == 0) return 1.0;
+    unsigned e = k < 0 ? (unsigned)(-k) : (unsigned)k;
+    double r = 1.0, b = x;
+    while (true) {
+      if (e & 1u) r = r * b;
+      e >>= 1;
+      if (!e) break;
+      b = b * b;
+    }
+    return k < 0 ? 1.0 / r : r;
+  }
+  void set_scal(int i, double v) {
+    hsmall_[0] = v;
+    cuda_check(cudaMemcpyAsync(scal_ + i, hsmall_, sizeof(double), cudaMemcpyHostToDevice, st_), "H2D scal");
+    sync();
+  }
+  double get_scal(int i) {
+    cuda_check(cudaMemcpyAsync(hsmall_, scal_ + i, sizeof(double), cudaMemcpyDeviceToHost, st_), "D2H scal");
+    sync();
+    return hsmall_[0];
+  }
+  void truncate_if_dirty() {
+    if (!dirty_) return;
+    specop(P_PS, P_PS, OP_TRUNC_RECT, 0.0);
+    specop(P_VZ, P_VZ, OP_TRUNC_RECT, 0.0);
+    dirty_ = false;
+  }
+  RandForceArgs make_rf_args(const RandForceHost* f) {
+    RandForceArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.nsq = (double)n_ * (double)n_;
+    for (int fi = 0; fi < 2; ++fi) {
+      RandForceField& d = a.f[fi];
+      d.nclear = prev_n_[fi];
+      for (int c = 0; c < prev_n_[fi]; ++c) d.clear[c] = prev_[fi][c];
+      d.nset = f[fi].nset;
+      for (int c = 0; c < f[fi].nset; ++c) {
+        d.set[c] = f[fi].set[c];
+        d.conj[c] = f[fi].conj[c];
+        prev_[fi][c] = f[fi].set[c];
+      }
+      prev_n_[fi] = f[fi].nset;
+      d.c0 = f[fi].c0;
+      d.kpow = f[fi].kpow;
+      d.cph = f[fi].cph;
+      d.sph = f[fi].sph;
+    }
+    return a;
+  }
+
+  // rf_mode: 0 none, 1 single args (rf), -1 sequence from the device array
+  void enqueue_step(const ModelCoef& mc, bool cfl_mode, double cfl, bool add_time, int rf_mode,
+                    const RandForceHost* rf) {
+    StepCoef sc{mc.nu, mc.hnu, mc.nuv, mc.hnuv, 2 * mc.omega, mc.nn, mc.mm, mc.nnv, mc.mmv};
+    cpx<T>* ps = planes_[P_PS];
+    cpx<T>* vz = planes_[P_VZ];
+    cpx<T>* c1 = planes_[P_C1];
+    cpx<T>* c2 = planes_[P_C2];
+    for (int o = 4; o >= 1; --o) {
+      const cpx<T>* in1 = o == 4 ? ps : c1;
+      const cpx<T>* in2 = o == 4 ? vz : c2;
+      cpx<T>* out1 = o == 1 ? ps : c1;
+      cpx<T>* out2 = o == 1 ? vz : c2;
+      if (ci_on_) {  // const_inj every substep (Rot2D3C.para.f90:565-569)
+        enqueue_const_inj(in1, o == 4 ? P_PS : P_C1, P_FP, 1, ci_fp0_);
+        enqueue_const_inj(in2, o == 4 ? P_VZ : P_C2, P_FZ, 0, ci_fz0_);
+      }
+      launch_passA(in1, in2);
+      if (o == 4 && cfl_mode) {
+        cuda_check(cudaMemsetAsync(enc_, 0, sizeof(unsigned long long), st_), "memset cfl");
+        launch_passB<true>(gd_.M);
+        k_cfl_dt<<<1, 1, 0, st_>>>(enc_, cfl_coef(cfl, mc), scal_, add_time ? 1 : 0);
+        post("k_cfl_dt");
+      } else {
+        launch_passB<false>(gd_.M);
+        if (o == 4 && add_time) {
+          k_add_time<<<1, 1, 0, st_>>>(scal_);
+          post("k_add_time");
+        }
+      }
+      if (o == 4 && rf_mode == 1) {
+        RandForceArgs a = make_rf_args(rf);
+        k_randforce<T><<<1, 1, 0, st_>>>(planes_[P_FP], planes_[P_FZ], scal_, a);
+        post("k_randforce");
+      } else if (o == 4 && rf_mode == -1) {
+        k_randforce_seq<T><<<1, 1, 0, st_>>>(planes_[P_FP], planes_[P_FZ], scal_, d_rf_, d_ctr_);
+        post("k_randforce_seq");
+      }
+      launch_passC(in1, in2, out1, out2, sc, o);
+    }
+  }
+
+  // ---------------------------------------------------------------- launchers
+  template <int DIR>
+  void launch_colfft(const cpx<T>* in, cpx<T>* out, int ncols) {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      auto k = k_colfft<T, N, DIR>;
+      k<<<(ncols + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(in, out, ncols, tw_);
+      post("k_colfft");
+    });
+  }
+  void launch_rowc2r(const cpx<T>* tin, T* rout, unsigned long long* mm) {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      auto k = k_rowc2r<T, N>;
+      k<<<(N / 2 + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(tin, rout, mm, tw_);
+      post("k_rowc2r");
+    });
+  }
+  void launch_rowr2c(const T* rin, cpx<T>* tout) {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      auto k = k_rowr2c<T, N>;
+      k<<<(N / 2 + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(rin, tout, tw_);
+      post("k_rowr2c");
+    });
+  }
+  void launch_passA(const cpx<T>* a, const cpx<T>* b) {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      auto k = k_passA<T, N>;
+      k<<<(gd_.M + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(a, b, tf_, gd_, tw_);
+      post("k_passA");
+    });
+  }
+  template <bool CFL>
+  void launch_passB(int kxo) {
+    const T inv4 = (T)(1.0 / ((double)n_ * n_ * n_ * n_));
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      auto k = k_passB<T, N, CFL>;
+      k<<<(N + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(tf_, pb_, kxo, gd_, inv4, tw_, enc_);
+      post("k_passB");
+    });
+  }
+  void launch_passC(const cpx<T>* c1in, const cpx<T>* c2in, cpx<T>* c1out, cpx<T>* c2out,
+                    const StepCoef& sc, int o) {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      auto k = k_passC<T, N>;
+      k<<<(gd_.M + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(
+          pb_, c1in, c2in, planes_[P_PS], planes_[P_VZ], planes_[P_FP], planes_[P_FZ], c1out, c2out, gd_, sc,
+          scal_, o, tw_);
+      post("k_passC");
+    });
+  }
+
+  // Dynamic shared memory above 48 KB has to be enabled per kernel before the
+  // first launch (and before any stream capture).
+  void set_kernel_attrs() {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      constexpr size_t sm = Cfg<T, N>::SMEM;
+      set_smem_attr(k_colfft<T, N, -1>, sm);
+      set_smem_attr(k_colfft<T, N, +1>, sm);
+      set_smem_attr(k_rowc2r<T, N>, sm);
+      set_smem_attr(k_rowr2c<T, N>, sm);
+      set_smem_attr(k_passA<T, N>, sm);
+      set_smem_attr(k_passB<T, N, true>, sm);
+      set_smem_attr(k_passB<T, N, false>, sm);
+      set_smem_attr(k_passC<T, N>, sm);
+    });
+  }
+
+  void build_twiddles() {
+    const int n = n_;
+    std::vector<double> c(n), s(n);
+    const double twopi = 2.0 * kPi;
+    for (int k = 0; k <= n / 8; ++k) {
+      const double a = twopi * (double)k / (double)n;
+      c[k] = std::cos(a);
+      s[k] = std::sin(a);
+    }
+    for (int k = n / 8 + 1; k <= n / 4; ++k) {
+      c[k] = s[n / 4 - k];
+      s[k] = c[n / 4 - k];
+    }
+    for (int k = n / 4 + 1; k <= n / 2; ++k) {
+      c[k] = -c[n / 2 - k];
+      s[k] = s[n / 2 - k];
+    }
+    for (int k = n / 2 + 1; k < n; ++k) {
+      c[k] = c[n - k];
+      s[k] = -s[n - k];
+    }
+    std::vector<tw_t<T>> h(n);
+    for (int k = 0; k < n; ++k) fill_tw(h[k], c[k], -s[k]);
+    cuda_check(cudaMemcpyAsync(tw_, h.data(), sizeof(tw_t<T>) * n, cudaMemcpyHostToDevice, st_), "H2D twiddles");
+    sync();
+  }
+  static void fill_tw(double2& w, double re, double im) {
+    w.x = re;
+    w.y = im;
+  }
+  static void fill_tw(float4& w, double re, double im) {
+    w.x = (float)re;
+    w.y = (float)im;
+    w.z = (float)(re - (double)w.x);
+    w.w = (float)(im - (double)w.y);
+  }
+
+  int n_, dev_;
+  bool full_;
+  cudaStream_t st_ = nullptr;
+  bool ci_on_ = false;
+  int ci_n_ = 0;
+  double ci_lo_ = 0, ci_hi_ = 0, ci_fp0_ = 0, ci_fz0_ = 0;
+  int* ci_idx_ = nullptr;
+  int* ci_mir_ = nullptr;
+  float* ci_rnd_ = nullptr;
+  DevGrid gd_{};
+  size_t S_ = 0, stage_count_ = 0, bytes_ = 0;
+  std::vector<void*> owned_;
+  cpx<T>* planes_[P_COUNT] = {};
+  T* rplanes_[R_COUNT] = {};
+  cpx<T>* tf_ = nullptr;
+  cpx<T>* pb_ = nullptr;
+  cpx<T>* tg_ = nullptr;
+  tw_t<T>* tw_ = nullptr;
+  double* stage64_ = nullptr;
+  double* scal_ = nullptr;
+  unsigned long long* enc_ = nullptr;
+  double* partials_ = nullptr;
+  double* small_ = nullptr;
+  double* hsmall_ = nullptr;
+  RandForceArgs* d_rf_ = nullptr;
+  int rf_cap_ = 0;
+  int* d_ctr_ = nullptr;
+  int prev_[2][4] = {};
+  int prev_n_[2] = {0, 0};
+  bool dirty_ = false;
+  int launches_ = 0;
+  cudaGraphExec_t graph_ = nullptr;
+  int graph_launches_ = 0;
+  GraphKey gkey_;
+};
+
+}  // namespace r2d3c

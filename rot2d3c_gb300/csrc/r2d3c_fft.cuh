@@ -1,0 +1,221 @@
+// Shared-memory / register block FFT for sm_103a.
+//
+// One length-N complex transform is carried by TPF = N/E threads.  Thread
+// `lane` holds v[q] = x[lane + q*TPF] (q < E) on entry and X[lane + q*TPF] on
+// exit, for every N and radix schedule: the same thread always owns the same
+// positions, which is what lets the bracket kernels form products of several
+// transforms in registers without another exchange.
+//
+// The schedule is a Stockham auto-sort: radix-E stages (the last one may have
+// a smaller radix), each an in-register DFT of R points followed by one padded
+// shared-memory exchange.  Twiddles come from a per-N table
+// tw[k] = exp(-2*pi*i*k/N) built on the host in FP64; the FP32 path stores
+// every twiddle as an (hi, lo) float pair and applies the low part with an
+// extra FMA ("compensated twiddles"), which removes the twiddle rounding from
+// the FP32 error budget.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace r2d3c {
+
+template <typename T> struct V2;
+template <> struct V2<double> { using t = double2; };
+template <> struct V2<float> { using t = float2; };
+template <typename T> using cpx = typename V2<T>::t;
+
+// Twiddle storage: FP64 -> (re, im); FP32 -> (re_hi, im_hi, re_lo, im_lo).
+template <typename T> struct TwS;
+template <> struct TwS<double> { using t = double2; };
+template <> struct TwS<float> { using t = float4; };
+template <typename T> using tw_t = typename TwS<T>::t;
+
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
+
+template <typename T>
+__device__ __forceinline__ cpx<T> mkc(T x, T y) {
+  cpx<T> r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+
+// a * w with w from the table; DIR = -1 uses w, DIR = +1 uses conj(w).
+template <int DIR>
+__device__ __forceinline__ double2 twmul(double2 a, double2 w) {
+  const double wy = DIR < 0 ? w.y : -w.y;
+  return make_double2(fma(a.x, w.x, -a.y * wy), fma(a.x, wy, a.y * w.x));
+}
+template <int DIR>
+__device__ __forceinline__ float2 twmul(float2 a, float4 w) {
+  const float wy = DIR < 0 ? w.y : -w.y;
+  const float ly = DIR < 0 ? w.w : -w.w;
+  const float tr = fmaf(a.x, w.z, -a.y * ly);
+  const float ti = fmaf(a.x, ly, a.y * w.z);
+  return make_float2(fmaf(a.x, w.x, fmaf(-a.y, wy, tr)),
+                     fmaf(a.x, wy, fmaf(a.y, w.x, ti)));
+}
+
+// Constant twiddle exp(DIR*2*pi*i*I16/16), I16 in [0,8).  The constants are
+// cos/sin of multiples of pi/8; the FP32 variant carries a low-order part.
+template <typename T, int I16, int DIR>
+__device__ __forceinline__ cpx<T> kmul(cpx<T> a) {
+  constexpr double C1 = 0.92387953251128675613;  // cos(pi/8)
+  constexpr double S1 = 0.38268343236508977173;  // sin(pi/8)
+  constexpr double R2 = 0.70710678118654752440;  // 1/sqrt(2)
+  if constexpr (I16 == 0) {
+    return a;
+  } else if constexpr (I16 == 4) {  // DIR * i
+    if constexpr (DIR > 0) return mkc<T>(-a.y, a.x);
+    else return mkc<T>(a.y, -a.x);
+  } else if constexpr (I16 == 2) {  // (1 + DIR i)/sqrt2
+    constexpr T s = (T)R2;
+    if constexpr (DIR > 0) return mkc<T>((a.x - a.y) * s, (a.y + a.x) * s);
+    else return mkc<T>((a.x + a.y) * s, (a.y - a.x) * s);
+  } else if constexpr (I16 == 6) {  // (-1 + DIR i)/sqrt2
+    constexpr T s = (T)R2;
+    if constexpr (DIR > 0) return mkc<T>((-a.x - a.y) * s, (a.x - a.y) * s);
+    else return mkc<T>((a.y - a.x) * s, (-a.x - a.y) * s);
+  } else {
+    constexpr double c = (I16 == 1) ? C1 : (I16 == 3) ? S1 : (I16 == 5) ? -S1 : -C1;
+    constexpr double s = (I16 == 1) ? S1 : (I16 == 3) ? C1 : (I16 == 5) ? C1 : S1;
+    constexpr double sd = DIR * s;
+    if constexpr (sizeof(T) == 8) {
+      return mkc<T>(fma(a.x, c, -a.y * sd), fma(a.x, sd, a.y * c));
+    } else {
+      constexpr float ch = (float)c, cl = (float)(c - (double)(float)c);
+      constexpr float sh = (float)sd, sl = (float)(sd - (double)(float)sd);
+      const float tr = fmaf(a.x, cl, -a.y * sl);
+      const float ti = fmaf(a.x, sl, a.y * cl);
+      return mkc<T>(fmaf(a.x, ch, fmaf(-a.y, sh, tr)), fmaf(a.x, sh, fmaf(a.y, ch, ti)));
+    }
+  }
+}
+
+// In-register DFT of R points: X[k] = sum_r u[r] exp(DIR*2*pi*i*r*k/R),
+// recursive radix-2 decimation in time, unrolled at compile time.
+template <typename T, int R, int DIR> struct RegDFT {
+  template <int K>
+  static __device__ __forceinline__ void bfly(cpx<T>* u, const cpx<T>* e, const cpx<T>* o) {
+    if constexpr (K < R / 2) {
+      const cpx<T> t = kmul<T, (K * 16) / R, DIR>(o[K]);
+      u[K] = mkc<T>(e[K].x + t.x, e[K].y + t.y);
+      u[K + R / 2] = mkc<T>(e[K].x - t.x, e[K].y - t.y);
+      bfly<K + 1>(u, e, o);
+    }
+  }
+  static __device__ __forceinline__ void run(cpx<T>* u) {
+    cpx<T> e[R / 2], o[R / 2];
+#pragma unroll
+    for (int i = 0; i < R / 2; ++i) {
+      e[i] = u[2 * i];
+      o[i] = u[2 * i + 1];
+    }
+    RegDFT<T, R / 2, DIR>::run(e);
+    RegDFT<T, R / 2, DIR>::run(o);
+    bfly<0>(u, e, o);
+  }
+};
+template <typename T, int DIR> struct RegDFT<T, 1, DIR> {
+  static __device__ __forceinline__ void run(cpx<T>*) {}
+};
+template <typename T, int DIR> struct RegDFT<T, 2, DIR> {
+  static __device__ __forceinline__ void run(cpx<T>* u) {
+    const cpx<T> a = u[0], b = u[1];
+    u[0] = mkc<T>(a.x + b.x, a.y + b.y);
+    u[1] = mkc<T>(a.x - b.x, a.y - b.y);
+  }
+};
+
+__device__ __forceinline__ int spad(int i) { return i + (i >> 5); }
+
+template <int TPF>
+__device__ __forceinline__ void fft_sync() {
+  if constexpr (TPF <= 32) {
+    __syncwarp();
+  } else {
+    __syncthreads();
+  }
+}
+
+template <typename T, int N, int E>
+struct BlockFFT {
+  static_assert((N & (N - 1)) == 0 && N >= E && E >= 2, "N, E powers of two");
+  static constexpr int TPF = N / E;
+  static constexpr int LOGN = ilog2(N);
+  static constexpr int LOGE = ilog2(E);
+  static constexpr int NST = (LOGN + LOGE - 1) / LOGE;
+  static constexpr int LAST_R = 1 << (LOGN - LOGE * (NST - 1));
+  static constexpr int SMEM_ELEMS = N + (N >> 5);  // per (re|im) array
+  static constexpr size_t SMEM_BYTES = 2 * SMEM_ELEMS * sizeof(T);
+
+  template <int DIR, int S, int NS>
+  static __device__ __forceinline__ void stage(cpx<T> (&v)[E], int lane, T* sre, T* sim,
+                                               const tw_t<T>* __restrict__ tw) {
+    constexpr int R = (S == NST - 1) ? LAST_R : E;
+    constexpr int B = E / R;
+    constexpr int LOGNS = ilog2(NS);
+#pragma unroll
+    for (int m = 0; m < B; ++m) {
+      const int j = lane + m * TPF;
+      const int jm = j & (NS - 1);
+      cpx<T> u[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) u[r] = v[m + r * B];
+      if constexpr (NS > 1) {
+        constexpr int STR = N / (NS * R);
+#pragma unroll
+        for (int r = 1; r < R; ++r) u[r] = twmul<DIR>(u[r], __ldg(&tw[r * jm * STR]));
+      }
+      RegDFT<T, R, DIR>::run(u);
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[m + r * B] = u[r];
+    }
+    if constexpr (S < NST - 1) {
+#pragma unroll
+      for (int m = 0; m < B; ++m) {
+        const int j = lane + m * TPF;
+        const int base = ((j >> LOGNS) << (LOGNS + ilog2(R))) + (j & (NS - 1));
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int idx = spad(base + r * NS);
+          sre[idx] = v[m + r * B].x;
+          sim[idx] = v[m + r * B].y;
+        }
+      }
+      fft_sync<TPF>();
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int idx = spad(lane + q * TPF);
+        v[q] = mkc<T>(sre[idx], sim[idx]);
+      }
+      fft_sync<TPF>();
+      stage<DIR, S + 1, NS * R>(v, lane, sre, sim, tw);
+    }
+  }
+
+  // X[k] = sum_x x[x] exp(DIR*2*pi*i*x*k/N), unnormalised.
+  template <int DIR>
+  static __device__ __forceinline__ void run(cpx<T> (&v)[E], int lane, T* sre, T* sim,
+                                             const tw_t<T>* __restrict__ tw) {
+    stage<DIR, 0, 1>(v, lane, sre, sim, tw);
+  }
+
+  // Write the natural-order result to shared memory so that any thread of
+  // the group can read X[k] and X[N-k] (Hermitian split of packed pairs).
+  static __device__ __forceinline__ void to_smem(const cpx<T> (&v)[E], int lane, T* sre, T* sim) {
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int idx = spad(lane + q * TPF);
+      sre[idx] = v[q].x;
+      sim[idx] = v[q].y;
+    }
+  }
+  static __device__ __forceinline__ cpx<T> from_smem(int k, const T* sre, const T* sim) {
+    const int idx = spad(k);
+    return mkc<T>(sre[idx], sim[idx]);
+  }
+};
+
+}  // namespace r2d3c

@@ -1,0 +1,423 @@
+// Device kernels of the Rot2D3C time-step hot path (sm_103a).
+//
+// Data layout in HBM (identical to the reference's Fortran arrays):
+//   spectral plane  C[kx][ky]  kx in [0, n/2], ky index j in [0, n), ky fastest
+//                   (Fortran C(n, n/2+1), fftp2D.f90:153)
+//   physical plane  R[y][x]    x fastest (Fortran R(n, n), fftp2D.f90:157)
+//   mixed plane     T[kx][y]   result of the y-direction transform of one kx
+//                   column, y fastest; used between the column and row passes
+//
+// Hot path of one RK substep (Rot2D3C.para.f90:571-599), three passes:
+//   A  per kx column (kx <= n/3): the six masked spectral derivatives
+//      d_x psi, d_y psi, d_x(-k^2 psi), d_y(-k^2 psi), d_x vz, d_y vz
+//      (derivk2/laplak2, pseudospec2D_Rot2D3C.f90:6-95) and their inverse
+//      y-FFTs -> 6 mixed planes.  Only |ky| <= n/3 is read (2/3 truncation).
+//   B  per physical row y: three packed complex x-IFFTs give the six real
+//      derivative rows (two real C2R per complex transform), the brackets
+//      [psi,-k^2 psi] and [psi,vz] (poisson, :169-226) are formed in
+//      registers, scaled by 1/n^4, and one packed forward x-FFT returns both
+//      to mixed space; only kx <= n/3 is written.  Substep 1 also takes the
+//      CFL maximum of |grad psi|^2 (CFL_condition, :862-876).
+//   C  per kx column: forward y-FFT of both brackets and the semi-implicit
+//      RK update with Coriolis coupling and forcing (Rot2D3C.para.f90:578-599).
+#pragma once
+
+#include "r2d3c_fft.cuh"
+
+namespace r2d3c {
+
+struct DevGrid {
+  int n;      // grid points per direction (power of two)
+  int nh;     // n/2 + 1 spectral columns
+  int L;      // floor(n/3): largest retained |kx|, |ky|
+  int M;      // L + 1 retained kx columns
+  int kmaxi;  // floor((n/3)^2): ka2 <= kmax  <=>  kx^2+ky^2 <= kmaxi
+};
+
+struct StepCoef {
+  double nu, hnu, nuv, hnuv, w2;  // w2 = 2*omega
+  int nn, mm, nnv, mmv;
+};
+
+template <typename T, int N>
+struct Cfg {
+  static constexpr int E = (N >= 8192) ? 16 : 8;
+  using FFT = BlockFFT<T, N, E>;
+  static constexpr int TPF = N / E;
+  static constexpr int G = TPF >= 256 ? 1 : 256 / TPF;  // transforms per CTA
+  static constexpr int THREADS = TPF * G;
+  static constexpr size_t SMEM = (size_t)G * FFT::SMEM_BYTES;
+};
+
+// ky value of row index j (Rot2D3C.para.f90:220-223)
+__device__ __forceinline__ int ky_of(int j, int n) { return j < (n >> 1) ? j : j - n; }
+
+template <typename T>
+__device__ __forceinline__ cpx<T> czero() {
+  return mkc<T>((T)0, (T)0);
+}
+
+// Non-negative double -> order-preserving 64-bit key for atomicMax (CFL max);
+// signed doubles use the sign-flip encoding below.
+__device__ __forceinline__ unsigned long long enc_ordered(double v) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
+}
+
+template <typename T>
+__device__ __forceinline__ T powi(T x, int k) {
+  if (k == 0) return (T)1;
+  unsigned e = k < 0 ? (unsigned)(-k) : (unsigned)k;
+  T r = (T)1, b = x;
+  while (true) {
+    if (e & 1u) r = r * b;
+    e >>= 1;
+    if (!e) break;
+    b = b * b;
+  }
+  return k < 0 ? (T)1 / r : r;
+}
+
+#define R2D3C_SMEM_DECL                                     \
+  extern __shared__ __align__(16) unsigned char smraw_[]; \
+  T* smbase_ = reinterpret_cast<T*>(smraw_);
+
+// --------------------------------------------------------------------------
+// generic y-direction transform of `ncols` contiguous columns of length N
+// (fftp2D.f90:208 forward, :251 inverse), in place allowed
+// --------------------------------------------------------------------------
+template <typename T, int N, int DIR>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
+  T* sim = sre + F::SMEM_ELEMS;
+  const int col = blockIdx.x * C::G + g;
+  const bool ok = col < ncols;
+  const cpx<T>* src = in + (size_t)(ok ? col : 0) * N;
+  cpx<T> v[C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) v[q] = ok ? src[lane + q * C::TPF] : czero<T>();
+  F::template run<DIR>(v, lane, sre, sim, tw);
+  if (ok) {
+    cpx<T>* dst = out + (size_t)col * N;
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[q];
+  }
+}
+
+// --------------------------------------------------------------------------
+// generic x-direction C2R of two rows (y0, y0+1) per transform: the two
+// Hermitian spectra are packed as Z = Xa + i Xb so one complex IFFT returns
+// row y0 in the real and row y0+1 in the imaginary part.  Im at kx = 0 and
+// kx = n/2 is ignored, as FFTW's complex-to-real does (fftp2D.f90:286).
+// Optionally stores the rows and/or folds them into a max/min.
+// --------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_rowc2r(const cpx<T>* __restrict__ tin, T* __restrict__ rout,
+         unsigned long long* __restrict__ mm_enc, const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
+  T* sim = sre + F::SMEM_ELEMS;
+  int pair = blockIdx.x * C::G + g;
+  const bool ok = pair < N / 2;
+  if (!ok) pair = 0;  // surplus groups recompute pair 0 and store nothing
+  const int y0 = 2 * pair;
+  cpx<T> v[C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int k = lane + q * C::TPF;
+    const int kk = k <= N / 2 ? k : N - k;
+    const cpx<T> a = tin[(size_t)kk * N + y0];
+    const cpx<T> b = tin[(size_t)kk * N + y0 + 1];
+    if (k == 0 || k == N / 2) {
+      v[q] = mkc<T>(a.x, b.x);
+    } else if (k < N / 2) {
+      v[q] = mkc<T>(a.x - b.y, a.y + b.x);
+    } else {
+      v[q] = mkc<T>(a.x + b.y, b.x - a.y);
+    }
+  }
+  F::template run<+1>(v, lane, sre, sim, tw);
+  if (rout && ok) {
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      const int x = lane + q * C::TPF;
+      rout[(size_t)y0 * N + x] = v[q].x;
+      rout[(size_t)(y0 + 1) * N + x] = v[q].y;
+    }
+  }
+  if (mm_enc) {
+    double mx = (double)v[0].x, mn = (double)v[0].x;
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      mx = fmax(mx, fmax((double)v[q].x, (double)v[q].y));
+      mn = fmin(mn, fmin((double)v[q].x, (double)v[q].y));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&mm_enc[0], enc_ordered(mx));
+      atomicMax(&mm_enc[1], enc_ordered(-mn));
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// generic x-direction R2C of two rows per transform (fftp2D.f90:171):
+// z = r[y0] + i r[y0+1]; Xa = (W[k] + conj W[N-k])/2, Xb = (W[k] - conj W[N-k])/2i
+// written to the mixed plane T[kx][y] for kx in [0, N/2].
+// --------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
+  T* sim = sre + F::SMEM_ELEMS;
+  int pair = blockIdx.x * C::G + g;
+  const bool ok = pair < N / 2;
+  if (!ok) pair = 0;
+  const int y0 = 2 * pair;
+  cpx<T> v[C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int x = lane + q * C::TPF;
+    v[q] = mkc<T>(rin[(size_t)y0 * N + x], rin[(size_t)(y0 + 1) * N + x]);
+  }
+  F::template run<-1>(v, lane, sre, sim, tw);
+  F::to_smem(v, lane, sre, sim);
+  fft_sync<C::TPF>();
+  const T h = (T)0.5;
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int k = lane + q * C::TPF;
+    if (ok && k <= N / 2) {
+      const cpx<T> w = F::from_smem(k, sre, sim);
+      const cpx<T> u = F::from_smem((N - k) & (N - 1), sre, sim);
+      tout[(size_t)k * N + y0] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
+      tout[(size_t)k * N + y0 + 1] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// pass A: masked derivatives + inverse y-FFT, 6 fields per kx column
+// --------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __restrict__ tf,
+        DevGrid gd, const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
+  T* sim = sre + F::SMEM_ELEMS;
+  const int col = blockIdx.x * C::G + g;
+  const bool ok = col < gd.M;
+  const size_t plane = (size_t)gd.M * N;
+  cpx<T> a[C::E], b[C::E];
+  T kyv[C::E], k2v[C::E];
+  const T kxv = (T)col;
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int j = lane + q * C::TPF;
+    const int ky = ky_of(j, N);
+    const int k2 = col * col + ky * ky;
+    const bool in = ok && (ky <= gd.L && -ky <= gd.L) && k2 <= gd.kmaxi;
+    a[q] = in ? ps[(size_t)col * N + j] : czero<T>();
+    b[q] = in ? vz[(size_t)col * N + j] : czero<T>();
+    kyv[q] = (T)ky;
+    k2v[q] = (T)k2;
+  }
+  cpx<T> v[C::E];
+#pragma unroll 1
+  for (int f = 0; f < 6; ++f) {
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
+      const T k = (f & 1) ? kyv[q] : kxv;
+      cpx<T> s;
+      if (f < 2) {
+        s = a[q];
+      } else if (f < 4) {
+        const T m = -k2v[q];  // laplak2: -ka2*a
+        s = mkc<T>(m * a[q].x, m * a[q].y);
+      } else {
+        s = b[q];
+      }
+      v[q] = mkc<T>(-k * s.y, k * s.x);
+    }
+    F::template run<+1>(v, lane, sre, sim, tw);
+    if (ok) {
+      cpx<T>* dst = tf + (size_t)f * plane + (size_t)col * N;
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[q];
+    }
+  }
+}
+
+// Packed spectrum of a pair of mixed planes (A, B) at row y for x-position k:
+// Z[k] = A[k] + i B[k] on the retained kx < M, conj-extended for k > N - M.
+template <typename T, int N>
+__device__ __forceinline__ cpx<T> packed_pair(const cpx<T>* __restrict__ pa,
+                                              const cpx<T>* __restrict__ pb, int k, int y, int M) {
+  if (k < M) {
+    const cpx<T> a = pa[(size_t)k * N + y];
+    const cpx<T> b = pb[(size_t)k * N + y];
+    if (k == 0) return mkc<T>(a.x, b.x);  // Im of the kx = 0 column is ignored
+    return mkc<T>(a.x - b.y, a.y + b.x);
+  }
+  if (k > N - M) {
+    const int kk = N - k;
+    const cpx<T> a = pa[(size_t)kk * N + y];
+    const cpx<T> b = pb[(size_t)kk * N + y];
+    return mkc<T>(a.x + b.y, b.x - a.y);
+  }
+  return czero<T>();
+}
+
+// --------------------------------------------------------------------------
+// pass B: per row, the two brackets in physical space and back to mixed space
+// --------------------------------------------------------------------------
+template <typename T, int N, bool CFL>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
+        const tw_t<T>* __restrict__ tw, unsigned long long* __restrict__ cfl_enc) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
+  T* sim = sre + F::SMEM_ELEMS;
+  int y = blockIdx.x * C::G + g;
+  const bool ok = y < N;
+  if (!ok) y = 0;  // surplus groups recompute row 0 and store nothing
+  const int M = gd.M;
+  const size_t plane = (size_t)M * N;
+  cpx<T> z1[C::E], v[C::E];
+  T p1[C::E];
+  // pair (d_x psi, d_y psi)
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) z1[q] = packed_pair<T, N>(tf, tf + plane, lane + q * C::TPF, y, M);
+  F::template run<+1>(z1, lane, sre, sim, tw);
+  if constexpr (CFL) {
+    double m = 0.0;
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      const double rx = (double)z1[q].x, ry = (double)z1[q].y;
+      m = fmax(m, rx * rx + ry * ry);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(cfl_enc, enc_ordered(m));
+  }
+  // pair (d_x(-k^2 psi), d_y(-k^2 psi)) -> [psi, -k^2 psi]
+#pragma unroll
+  for (int q = 0; q < C::E; ++q)
+    v[q] = packed_pair<T, N>(tf + 2 * plane, tf + 3 * plane, lane + q * C::TPF, y, M);
+  F::template run<+1>(v, lane, sre, sim, tw);
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) p1[q] = (z1[q].x * v[q].y - z1[q].y * v[q].x) * inv_n4;
+  // pair (d_x vz, d_y vz) -> [psi, vz]
+#pragma unroll
+  for (int q = 0; q < C::E; ++q)
+    v[q] = packed_pair<T, N>(tf + 4 * plane, tf + 5 * plane, lane + q * C::TPF, y, M);
+  F::template run<+1>(v, lane, sre, sim, tw);
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) v[q] = mkc<T>(p1[q], (z1[q].x * v[q].y - z1[q].y * v[q].x) * inv_n4);
+  // forward x-FFT of both real products at once
+  F::template run<-1>(v, lane, sre, sim, tw);
+  F::to_smem(v, lane, sre, sim);
+  fft_sync<C::TPF>();
+  const size_t oplane = (size_t)gd.nh * N;
+  const T h = (T)0.5;
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int k = lane + q * C::TPF;
+    if (ok && k < kxo) {
+      const cpx<T> w = F::from_smem(k, sre, sim);
+      const cpx<T> u = F::from_smem((N - k) & (N - 1), sre, sim);
+      pb[(size_t)k * N + y] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
+      pb[oplane + (size_t)k * N + y] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// pass C: forward y-FFT of both brackets + RK substep update
+// (Rot2D3C.para.f90:578-599).  c1in/c2in may alias c1out/c2out, and in the
+// last substep c1out/c2out are ps/vz themselves: every element is read and
+// written by the same thread.
+// --------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
+        const cpx<T>* ps, const cpx<T>* vz, const cpx<T>* __restrict__ fp,
+        const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out, DevGrid gd, StepCoef sc,
+        const double* __restrict__ dtp, int o, const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
+  T* sim = sre + F::SMEM_ELEMS;
+  const int col = blockIdx.x * C::G + g;
+  const bool ok = col < gd.M;
+  const size_t oplane = (size_t)gd.nh * N;
+  const cpx<T>* s5 = pb + (size_t)(ok ? col : 0) * N;
+  cpx<T> c5[C::E], c6[C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    c5[q] = s5[lane + q * C::TPF];
+    c6[q] = s5[oplane + lane + q * C::TPF];
+  }
+  F::template run<-1>(c5, lane, sre, sim, tw);
+  F::template run<-1>(c6, lane, sre, sim, tw);
+  if (!ok) return;
+  const T tmp1 = (T)(*dtp / (double)o);  // :581
+  const T nu = (T)sc.nu, hnu = (T)sc.hnu, nuv = (T)sc.nuv, hnuv = (T)sc.hnuv, w2 = (T)sc.w2;
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int j = lane + q * C::TPF;
+    const int ky = ky_of(j, N);
+    if (ky > gd.L || -ky > gd.L) continue;
+    const size_t idx = (size_t)col * N + j;
+    const int k2 = col * col + ky * ky;
+    cpx<T> n1 = czero<T>(), n2 = czero<T>();
+    if (k2 <= gd.kmaxi && k2 >= 1) {  // ka2 <= kmax .and. ka2 > tiny (:580)
+      const cpx<T> a1 = c1in[idx], a2 = c2in[idx];
+      const T kyf = (T)ky, ka2 = (T)k2;
+      const cpx<T> C3 = mkc<T>(-kyf * a1.y, kyf * a1.x);  // derivk2(C1,C3,2)
+      const cpx<T> C4 = mkc<T>(-kyf * a2.y, kyf * a2.x);  // derivk2(C2,C4,2)
+      const T tmp2 = (T)1 / ka2;
+      const T tmp3 = (T)1 + (nu * powi(ka2, sc.nn) + hnu * powi(tmp2, sc.mm)) * tmp1;
+      const cpx<T> p0 = ps[idx], f0 = fp[idx];
+      const T u1x = p0.x + ((-c5[q].x + w2 * C4.x) * tmp2 + f0.x) * tmp1;
+      const T u1y = p0.y + ((-c5[q].y + w2 * C4.y) * tmp2 + f0.y) * tmp1;
+      n1 = mkc<T>(u1x / tmp3, u1y / tmp3);
+      const T tmp3v = (T)1 + (nuv * powi(ka2, sc.nnv) + hnuv * powi(tmp2, sc.mmv)) * tmp1;
+      const cpx<T> v0 = vz[idx], g0 = fz[idx];
+      const T u2x = v0.x + (c6[q].x + w2 * C3.x + g0.x) * tmp1;
+      const T u2y = v0.y + (c6[q].y + w2 * C3.y + g0.y) * tmp1;
+      n2 = mkc<T>(u2x / tmp3v, u2y / tmp3v);
+    }
+    c1out[idx] = n1;
+    c2out[idx] = n2;
+  }
+}
+
+}  // namespace r2d3c
