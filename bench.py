@@ -1,0 +1,436 @@
+#!/usr/bin/env python
+"""Benchmark of the Rot2D3C RK4 time step on GB300.
+
+Workload: a single large run at n = 4096^2, RK order 4, fixed dt = 1e-4,
+nu = nuv = 1e-5 (nn = 1), hypoviscosity hnu = hnuv = 0.1 (nabla^-4, mm = 2),
+Omega = 10, a seeded random-phase initial spectrum ~ k^-3 for 1 <= |k| <= 100
+(energy(ps,1) = energy(vz,0) = 0.5) and a seeded, time-constant random-phase
+forcing in the shell 20 <= |k| <= 22 normalised like iflow = 1
+(energy(fp,1) = energy(fz,0) = 1).  All inputs are synthetic.
+
+One bench step = one RK4 step.  The headline `value` is the FP32 path
+(FP32 fields and transforms with compensated twiddles, FP64 reductions); the
+FP64 drop-in path is measured on the same workload and reported in `fp64`,
+with the relative L2 error of omega and vz of the FP32 path against FP64
+after 100 steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: one field does not shard (replicas only); under torchrun every
+rank runs its own replica and `value` counts the steps of all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK steps/s at 4096^2 FP64 vs FP32 (err vs FP64); batched runs/s; LES-vs-DNS gain"
+UNIT = "RK4 steps/s"
+WORKLOAD = dict(n=4096, dt=1e-4, nu=1e-5, hnu=0.1, nn=1, mm=2, omega=10.0, ic_kmin=1.0,
+                ic_kmax=100.0, ic_slope=-3.0, f_kmin=20.0, f_kmax=22.0, ic_seed=1, f_seed=2)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=WORKLOAD["n"])
+    ap.add_argument("--fp64-steps", type=int, default=0, help="timed FP64 steps (default: --steps)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--err-steps", type=int, default=100)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- inputs
+def _grid(n):
+    import numpy as np
+    h = n // 2
+    ka = np.concatenate([np.arange(h), np.arange(h) - h]).astype(np.float64)
+    kx = ka[: h + 1]
+    return ka, kx, kx[:, None] ** 2 + ka[None, :] ** 2
+
+
+def _energy(a, ka2, kin, n):
+    import numpy as np
+    two = np.full((a.shape[0], 1), 2.0)
+    two[0, 0] = 1.0
+    return float(np.sum(two * np.abs(a) ** 2 * ka2 ** kin) / float(n) ** 4)
+
+
+def synthetic_field(n, kmin, kmax, amp_slope, seed):
+    """Random-phase spectral field in [kx][ky] layout with |a(k)| ~ k**amp_slope
+    on kmin <= |k| <= kmax; the kx = 0 column is made Hermitian."""
+    import numpy as np
+    ka, kx, ka2 = _grid(n)
+    rng = np.random.default_rng(seed)
+    k = np.sqrt(ka2)
+    shell = (k >= kmin) & (k <= kmax)
+    amp = np.where(shell, np.where(k > 0, k, 1.0) ** amp_slope, 0.0)
+    a = amp * np.exp(1j * rng.uniform(0.0, 2.0 * np.pi, size=ka2.shape))
+    col = a[0]
+    j = np.arange(1, n // 2)
+    col[n - j] = np.conj(col[j])
+    col[0] = col[0].real
+    col[n // 2] = 0.0
+    a[0] = col
+    return a, ka2
+
+
+def workload_inputs(n):
+    """(ps, vz, fp, fz) of the 4096^2 workload (scaled to n for smaller runs)."""
+    import numpy as np
+    w = WORKLOAD
+    s = n / 4096.0
+    # energy spectrum E(k) ~ k^-3: |psi| ~ k^-3 (E ~ k^3 |psi|^2), |vz| ~ k^-2
+    ps, ka2 = synthetic_field(n, w["ic_kmin"], max(w["ic_kmax"] * s, 4.0), w["ic_slope"], w["ic_seed"])
+    vz, _ = synthetic_field(n, w["ic_kmin"], max(w["ic_kmax"] * s, 4.0), w["ic_slope"] + 1.0, w["ic_seed"] + 100)
+    ps *= math.sqrt(0.5 / _energy(ps, ka2, 1, n))
+    vz *= math.sqrt(0.5 / _energy(vz, ka2, 0, n))
+    fkmin, fkmax = max(w["f_kmin"] * s, 2.0), max(w["f_kmax"] * s, 3.0)
+    fp, _ = synthetic_field(n, fkmin, fkmax, 0.0, w["f_seed"])
+    fz, _ = synthetic_field(n, fkmin, fkmax, 0.0, w["f_seed"] + 100)
+    fp *= math.sqrt(1.0 / _energy(fp, ka2, 1, n))
+    fz *= math.sqrt(1.0 / _energy(fz, ka2, 0, n))
+    return ps, vz, fp, fz, ka2
+
+
+def make_cparams(n):
+    import rot2d3c_gb300 as R
+    w = WORKLOAD
+    return R.make_params(n=n, nu=w["nu"], hnu=w["hnu"], nn=w["nn"], mm=w["mm"], nuv=w["nu"],
+                         hnuv=w["hnu"], nnv=w["nn"], mmv=w["mm"], omega=w["omega"], iflow=0,
+                         kup=w["f_kmax"], kdn=w["f_kmin"])
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        for line in (self.out or "").splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                "sw_power_cap"), parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- helpers
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def pass_bytes(n, real_bytes):
+    """Algorithmic HBM bytes per launch of passes A, B, C (one substep).
+    M = n/3+1 retained kx columns, K = 2(n/3)+1 retained ky rows, c = complex
+    element size.  A reads psi, vz on M x K and writes 6 mixed planes M x n;
+    B reads the 6 planes and writes 2; C reads 2 planes + c1, c2, ps, vz,
+    fp, fz on M x K and writes c1, c2 on M x K."""
+    L = n // 3
+    M, K = L + 1, 2 * L + 1
+    c = 2 * real_bytes
+    return {"A": (2 * M * K + 6 * M * n) * c, "B": (6 * M * n + 2 * M * n) * c,
+            "C": (2 * M * n + 6 * M * K + 2 * M * K) * c}
+
+
+def fft_flops_per_step(n):
+    """Nominal FFT FLOPs of one RK4 step of the fused path (5 L log2 L per
+    complex transform of length L): per substep 6 M column IFFTs (A), 4 n
+    packed row transforms (B), 2 M column FFTs (C)."""
+    M = n // 3 + 1
+    per = 5.0 * n * math.log2(n)
+    return 4 * (6 * M + 4 * n + 2 * M) * per
+
+
+def rel_err_fields(a_ps, a_vz, b_ps, b_vz, ka2):
+    """Relative L2 errors of omega = k^2 psi and vz (half-plane weighted)."""
+    import numpy as np
+    two = np.full((a_ps.shape[0], 1), 2.0)
+    two[0, 0] = 1.0
+
+    def rl2(x, y):
+        return float(np.sqrt(np.sum(two * np.abs(x - y) ** 2) / np.sum(two * np.abs(y) ** 2)))
+    return rl2(ka2 * a_ps, ka2 * b_ps), rl2(a_vz, b_vz)
+
+
+def timed_advance(ctx, steps, dt, torch):
+    """Device time of `steps` graph-replayed RK4 steps (CUDA events on the
+    context's stream)."""
+    import rot2d3c_gb300 as R
+    st = torch.cuda.ExternalStream(ctx.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    l0 = ctx.kernel_launches()
+    e0.record(st)
+    ctx.advance(steps, R.DT_FIXED, dt)
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3, ctx.kernel_launches() - l0
+
+
+def dist_barrier(torch, world):
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def dist_max(torch, world, v):
+    if world <= 1:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_baseline(n, ps, vz, fp, fz, budget_s=20.0):
+    """The C/OpenMP restatement of the reference step (oracle/cpu) on all host
+    cores: a bounded sample of the same workload."""
+    from oracle import cpu_oracle as CO
+    from oracle import rot2d3c_oracle as O
+    w = WORKLOAD
+    p = O.Params(n=n, nu=w["nu"], hnu=w["hnu"], nn=w["nn"], mm=w["mm"], nuv=w["nu"], hnuv=w["hnu"],
+                 nnv=w["nn"], mmv=w["mm"], omega=w["omega"], iflow=0)
+    th = CO.max_threads()
+    t0 = time.perf_counter()
+    a, b, _ = CO.run(p, ps, vz, fp, fz, 1, w["dt"], False, th)
+    t1 = time.perf_counter()
+    per = t1 - t0
+    k = max(1, min(20, int(budget_s / max(per, 1e-6)) - 1))
+    t0 = time.perf_counter()
+    CO.run(p, a, b, fp, fz, k, w["dt"], False, th)
+    dt = time.perf_counter() - t0
+    return {"value": k / dt, "unit": UNIT, "cores": th, "kind": "port",
+            "sample": f"{k} RK4 steps at {n}^2 FP64 (after 1 untimed), C/OpenMP restatement of the "
+                      f"reference step (35 C2R + 8 R2C per step as in the reference), {th} threads, "
+                      "MPI ranks: 1 (threads instead of MPI)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    n = args.n
+    ps, vz, fp, fz, _ = workload_inputs(n)
+    from oracle import cpu_oracle as CO
+    from oracle import rot2d3c_oracle as O
+    w = WORKLOAD
+    p = O.Params(n=n, nu=w["nu"], hnu=w["hnu"], nn=w["nn"], mm=w["mm"], nuv=w["nu"], hnuv=w["hnu"],
+                 nnv=w["nn"], mmv=w["mm"], omega=w["omega"], iflow=0)
+    th = CO.max_threads()
+    warm = max(0, min(args.warmup, 1))
+    a, b = ps, vz
+    if warm:
+        a, b, _ = CO.run(p, a, b, fp, fz, warm, w["dt"], False, th)
+    # bounded sample: at most args.steps steps or ~60 s of CPU work
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.steps:
+        a, b, _ = CO.run(p, a, b, fp, fz, 1, w["dt"], False, th)
+        done += 1
+        if time.perf_counter() - t0 > 60.0:
+            break
+    el = time.perf_counter() - t0
+    v = done / el
+    sample = (f"{done} of {args.steps} requested RK4 steps at {n}^2 FP64 (bounded to ~60 s), "
+              f"C/OpenMP restatement of the reference step, {th} threads, MPI ranks: 1")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": done, "warmup": warm, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"single run {n}^2, RK4, dt=1e-4 fixed, nu=1e-5, hnu=0.1, Omega=10, "
+                                   "IC k^-3 1<=|k|<=100, forcing shell 20-22", "n": n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- main arm
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import numpy as np
+    import torch
+    if world > 1:
+        torch.cuda.set_device(0)
+        torch.distributed.init_process_group("nccl")
+    import rot2d3c_gb300 as R
+    from rot2d3c_gb300 import build as B
+    B.build()
+    R.load()
+
+    n = args.n
+    dt = WORKLOAD["dt"]
+    K, W = args.steps, max(3, args.warmup)
+    ps, vz, fp, fz, ka2 = workload_inputs(n)
+    cp = make_cparams(n)
+
+    # ---- FP32 path: accuracy run, then timing
+    c32 = R.Context(cp, R.FP32)
+    c32.set_state(ps, vz)
+    c32.set_forcing(fp, fz)
+    out = {}
+    if not args.no_fp64:
+        c64 = R.Context(cp, R.FP64)
+        c64.set_state(ps, vz)
+        c64.set_forcing(fp, fz)
+        c64.advance(args.err_steps, R.DT_FIXED, dt)
+        c32.advance(args.err_steps, R.DT_FIXED, dt)
+        a64, b64 = c64.get_state()
+        a32, b32 = c32.get_state()
+        ew, ev = rel_err_fields(a32, b32, a64, b64, ka2)
+        out["err"] = {"rel_l2_omega": ew, "rel_l2_vz": ev, "after_steps": args.err_steps}
+        del a64, b64, a32, b32
+
+    c32.advance(W, R.DT_FIXED, dt)
+    dist_barrier(torch, world)
+    with ClockSampler(local if world == 1 else 0) as clk:
+        el32, launches32 = timed_advance(c32, K, dt, torch)
+        dist_barrier(torch, world)
+    el32 = dist_max(torch, world, el32)
+    clocks = clk.summary()
+
+    # per-pass device times (CUDA events around each launch, separate pass)
+    ms32, cnt32 = c32.profile_passes(min(K, 20), dt)
+    hbm, peak_kind = measured_peaks()
+    pb = pass_bytes(n, 4)
+    passes = {k: {"ms_per_launch": ms32[i], "algorithmic_bytes": pb[k],
+                  "achieved_gbs": pb[k] / (ms32[i] * 1e-3) / 1e9 if ms32[i] > 0 else None}
+              for i, k in enumerate("ABC")}
+    top = max("ABC", key=lambda k: passes[k]["ms_per_launch"])
+    ach = passes[top]["achieved_gbs"]
+    roofline = {"bound": "hbm", "kernel": f"k_pass{top} (FP32, n={n})", "achieved": ach, "peak": hbm,
+                "unit": "GB/s", "frac": ach / hbm, "peak_source": peak_kind,
+                "traffic": None, "passes": passes,
+                "step_share": {k: ms32[i] * cnt32[i] / sum(ms32[j] * cnt32[j] for j in range(4))
+                               for i, k in enumerate("ABC")}}
+
+    # ---- FP64 drop-in path
+    fp64 = None
+    if not args.no_fp64:
+        K64 = args.fp64_steps or K
+        c64.advance(W, R.DT_FIXED, dt)
+        el64, l64 = timed_advance(c64, K64, dt, torch)
+        el64 = dist_max(torch, world, el64)
+        ms64, cnt64 = c64.profile_passes(min(K64, 4), dt)
+        peak64 = R.fp64_fma_peak()
+        flops = fft_flops_per_step(n)
+        v64 = world * K64 / el64
+        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el64 / K64, "steps": K64,
+                "dtype": "f64", "fp32_speedup": (world * K / el32) / v64,
+                "roofline": {"bound": "fp64", "achieved": flops * K64 / el64 / 1e12,
+                             "peak": peak64, "unit": "TFLOP/s",
+                             "frac": flops * K64 / el64 / 1e12 / peak64,
+                             "note": "nominal FFT FLOPs (5 L log2 L) per step / step time; peak "
+                                     "= measured FP64 FMA throughput on this GPU"},
+                "passes_ms_per_launch": dict(zip("ABC", ms64[:3]))}
+        fp64.update(out.get("err", {}))
+        c64.destroy()
+
+    # ---- e2e through the C-ABI with host buffers (FP32 path)
+    e2e_steps = min(K, 50)
+    c32.synchronize()
+    t0 = time.perf_counter()
+    c32.set_state(ps, vz)                       # H2D of the state (host FP64 arrays)
+    for _ in range(e2e_steps):
+        c32.advance(1, R.DT_FIXED, dt)          # H2D dt, launch, D2H time and dt
+    a_out, b_out = c32.get_state()              # D2H of the state
+    el_e2e = time.perf_counter() - t0
+    el_e2e = dist_max(torch, world, el_e2e)
+    S = (n // 2 + 1) * n * 16
+    e2e = {"value": world * e2e_steps / el_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": (2 * S + 8 * e2e_steps) / e2e_steps,
+           "d2h_bytes_per_step": (2 * S + 16 * e2e_steps) / e2e_steps,
+           "steps": e2e_steps,
+           "path": "r2d3c_set_state + per-step r2d3c_advance(1) + r2d3c_get_state (host FP64 buffers)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(n, ps, vz, fp, fz)
+
+    v32 = world * K / el32
+    line = {"metric": METRIC, "value": v32, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * el32 / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 reductions)", "data": "synthetic",
+            "config": {"workload": f"single run {n}^2, RK4, dt=1e-4 fixed, nu=1e-5, hnu=0.1 (mm=2), "
+                                   "Omega=10, IC k^-3 1<=|k|<=100, forcing shell 20-22",
+                       "n": n, "precision": "FP32 path (headline) and FP64 path (fp64)",
+                       "l2": "working set larger than L2 (6 mixed planes of 268 MB at 4096^2 FP32)",
+                       "parallelism": f"replicas x{world}"},
+            "gpu_launches": launches32, "roofline": roofline, "clocks": clocks, "e2e": e2e,
+            "fp64": fp64, "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    c32.destroy()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

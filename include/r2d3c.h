@@ -188,6 +188,19 @@ int r2d3c_inerprod(r2d3c_ctx* ctx, const double* a, const double* b, int kin, do
 /* randu (pseudospec2D_mod.f90:142-161): one draw, *seed updated */
 float r2d3c_randu(int* seed);
 
+/* ---- measurement ------------------------------------------------------ */
+/* Average device time per launch of the three passes of the RK substep
+   (ms_per_launch[0] pass A, [1] pass B, [2] pass C, [3] other kernels) over
+   nsteps steps with a fixed dt, from CUDA events recorded on the context
+   stream around every launch; launches[4] receives the launch counts.
+   No counterpart in the reference (it has no timers). */
+int r2d3c_profile_passes(r2d3c_ctx* ctx, int nsteps, double dt, double* ms_per_launch,
+                         long long* launches);
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (dependent
+   FMA chains on every SM), the denominator of the FP64 path's roofline.
+   No counterpart in the reference. */
+int r2d3c_fp64_fma_peak(double* tflops);
+
 /* Device pointer of a context plane for GPU-resident callers:
    which = 0 ps, 1 vz, 2 fp, 3 fz (spectral planes of the context's compute
    type, complex interleaved [kx][ky]). */

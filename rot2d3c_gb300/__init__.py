@@ -63,6 +63,13 @@ def randu(seed: list) -> float:
     return float(np.float32(r))
 
 
+def fp64_fma_peak() -> float:
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    t = C.c_double()
+    check(load().r2d3c_fp64_fma_peak(C.byref(t)), "fp64_fma_peak")
+    return t.value
+
+
 def make_params(**kw) -> Params:
     """r2d3c_params with the reference's parameter.inp defaults overridden by kw."""
     d = dict(n=64, cfl=0.5, step=1, cstep=100, sstep=1000, tstep=10000, fp0=1.0, fz0=1.0,
@@ -281,6 +288,13 @@ class Context:
         return r.value
 
     # ---------------------------------------------------------------- misc
+    def profile_passes(self, nsteps: int, dt: float):
+        """(ms per launch [A, B, C, other], launches [A, B, C, other])."""
+        ms = (C.c_double * 4)()
+        cnt = (C.c_longlong * 4)()
+        check(load().r2d3c_profile_passes(self._h, nsteps, dt, ms, cnt), "profile_passes")
+        return list(ms), list(cnt)
+
     def kernel_launches(self) -> int:
         c = C.c_longlong()
         check(load().r2d3c_kernel_launches(self._h, C.byref(c)), "kernel_launches")

@@ -97,6 +97,8 @@ SIGNATURES = {
     "r2d3c_energy": (C.c_int, [_P, _D, C.c_int, _D]),
     "r2d3c_inerprod": (C.c_int, [_P, _D, _D, C.c_int, _D]),
     "r2d3c_randu": (C.c_float, [_I]),
+    "r2d3c_profile_passes": (C.c_int, [_P, C.c_int, C.c_double, _D, C.POINTER(C.c_longlong)]),
+    "r2d3c_fp64_fma_peak": (C.c_int, [_D]),
     "r2d3c_dev_ptr": (C.c_int, [_P, C.c_int, C.POINTER(_P)]),
     "r2d3c_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "r2d3c_synchronize": (C.c_int, [_P]),

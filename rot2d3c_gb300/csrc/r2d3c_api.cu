@@ -657,6 +657,65 @@ int r2d3c_inerprod(r2d3c_ctx* ctx, const double* a, const double* b, int kin, do
   API_END
 }
 
+int r2d3c_profile_passes(r2d3c_ctx* ctx, int nsteps, double dt, double* ms_per_launch,
+                         long long* launches) {
+  API_BEGIN
+  REQUIRE(ctx && ms_per_launch && launches, "NULL argument");
+  REQUIRE(nsteps >= 1, "nsteps must be >= 1");
+  REQUIRE(dt > 0.0 && std::isfinite(dt), "dt must be positive and finite");
+  REQUIRE(ctx->p.iflow != 2, "profiling covers the step without const_inj");
+  ctx->eng->set_dt(dt);
+  double ms[4];
+  ctx->eng->profile_steps(ctx->mc(), nsteps, ms, launches);
+  for (int k = 0; k < 4; ++k) ms_per_launch[k] = launches[k] ? ms[k] / (double)launches[k] : 0.0;
+  API_END
+}
+
+namespace {
+// Dependent FMA chains: 8 independent accumulators per thread, `iters`
+// iterations of 8 FMAs each.  The result is stored so nothing is elided.
+__global__ void k_fp64_fma(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = (double)(threadIdx.x + i) * 1e-3;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = fma(x[i], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += x[i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+int r2d3c_fp64_fma_peak(double* tflops) {
+  API_BEGIN
+  REQUIRE(tflops, "NULL argument");
+  int dev = 0, sms = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  double* d = nullptr;
+  cuda_check(cudaMalloc(&d, sizeof(double) * (size_t)blocks * threads), "cudaMalloc");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp64_fma<<<blocks, threads>>>(d, 64, 0.999999, 1e-7);  // warm-up
+  cudaEventRecord(e0);
+  k_fp64_fma<<<blocks, threads>>>(d, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  const cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  cuda_check(err, "fp64 peak kernel");
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  API_END
+}
+
 int r2d3c_dev_ptr(r2d3c_ctx* ctx, int which, void** ptr) {
   API_BEGIN
   REQUIRE(ctx && ptr, "NULL argument");

@@ -106,6 +106,11 @@ class IEngine {
   virtual void const_inj(int src, int dst, int kin, double f0) = 0;
   virtual void sync() = 0;
   virtual int kernel_launches() const = 0;
+  // Per-kernel device time of nsteps RK4 steps with the dt already set,
+  // measured with CUDA events recorded on the engine stream around every
+  // launch: ms[k] = total milliseconds, cnt[k] = launches, for k = 0 pass A,
+  // 1 pass B, 2 pass C, 3 everything else.
+  virtual void profile_steps(const ModelCoef& mc, int nsteps, double ms[4], long long cnt[4]) = 0;
 };
 
 // full = false allocates only what the Level-1 transforms need.

@@ -446,6 +446,38 @@ class EngineT final : public IEngine {
   }
   void sync() override { cuda_check(cudaStreamSynchronize(st_), "cudaStreamSynchronize"); }
 
+  void profile_steps(const ModelCoef& mc, int nsteps, double ms[4], long long cnt[4]) override {
+    truncate_if_dirty();
+    for (int k = 0; k < 4; ++k) {
+      ms[k] = 0.0;
+      cnt[k] = 0;
+    }
+    prof_.clear();
+    profiling_ = true;
+    try {
+      for (int s = 0; s < nsteps; ++s) enqueue_step(mc, false, 0.0, false, 0, nullptr);
+    } catch (...) {
+      profiling_ = false;
+      for (auto& e : prof_) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+      }
+      prof_.clear();
+      throw;
+    }
+    profiling_ = false;
+    sync();
+    for (auto& e : prof_) {
+      float t = 0.f;
+      cuda_check(cudaEventElapsedTime(&t, e.a, e.b), "cudaEventElapsedTime");
+      ms[e.kind] += t;
+      cnt[e.kind] += 1;
+      cudaEventDestroy(e.a);
+      cudaEventDestroy(e.b);
+    }
+    prof_.clear();
+  }
+
  private:
   static constexpr int kSumBlocks = 304;  // 2 CTAs per SM on 152 SMs
   static constexpr double kPi = 3.1415926535897932384;
@@ -498,6 +530,25 @@ class EngineT final : public IEngine {
   void post(const char* what) {
     ++launches_;
     cuda_check(cudaGetLastError(), what);
+  }
+  struct ProfEv {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  // brackets one launch with events when profiling (kind: 0 A, 1 B, 2 C, 3 other)
+  template <typename F>
+  void timed(int kind, F&& launch) {
+    if (!profiling_) {
+      launch();
+      return;
+    }
+    ProfEv e{kind, nullptr, nullptr};
+    cuda_check(cudaEventCreate(&e.a), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&e.b), "cudaEventCreate");
+    prof_.push_back(e);
+    cuda_check(cudaEventRecord(e.a, st_), "cudaEventRecord");
+    launch();
+    cuda_check(cudaEventRecord(e.b, st_), "cudaEventRecord");
   }
   template <typename S, typename D>
   void convert(const S* src, D* dst, size_t count) {
@@ -578,14 +629,14 @@ class EngineT final : public IEngine {
         enqueue_const_inj(in1, o == 4 ? P_PS : P_C1, P_FP, 1, ci_fp0_);
         enqueue_const_inj(in2, o == 4 ? P_VZ : P_C2, P_FZ, 0, ci_fz0_);
       }
-      launch_passA(in1, in2);
+      timed(0, [&] { launch_passA(in1, in2); });
       if (o == 4 && cfl_mode) {
         cuda_check(cudaMemsetAsync(enc_, 0, sizeof(unsigned long long), st_), "memset cfl");
         launch_passB<true>(gd_.M);
         k_cfl_dt<<<1, 1, 0, st_>>>(enc_, cfl_coef(cfl, mc), scal_, add_time ? 1 : 0);
         post("k_cfl_dt");
       } else {
-        launch_passB<false>(gd_.M);
+        timed(1, [&] { launch_passB<false>(gd_.M); });
         if (o == 4 && add_time) {
           k_add_time<<<1, 1, 0, st_>>>(scal_);
           post("k_add_time");
@@ -599,7 +650,7 @@ class EngineT final : public IEngine {
         k_randforce_seq<T><<<1, 1, 0, st_>>>(planes_[P_FP], planes_[P_FZ], scal_, d_rf_, d_ctr_);
         post("k_randforce_seq");
       }
-      launch_passC(in1, in2, out1, out2, sc, o);
+      timed(2, [&] { launch_passC(in1, in2, out1, out2, sc, o); });
     }
   }
 
@@ -752,6 +803,8 @@ class EngineT final : public IEngine {
   int launches_ = 0;
   cudaGraphExec_t graph_ = nullptr;
   int graph_launches_ = 0;
+  bool profiling_ = false;
+  std::vector<ProfEv> prof_;
   GraphKey gkey_;
 };
 
