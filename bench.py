@@ -233,12 +233,20 @@ def dist_barrier(torch, world):
         torch.distributed.barrier()
 
 
-def dist_max(torch, world, v):
+def dist_max(torch, world, v, device="cuda"):
+    """Max over ranks (the slowest replica sets the job's time)."""
     if world <= 1:
         return v
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(torch, world, steps_per_rank, elapsed_s, device="cuda"):
+    """Whole-job steps/s of `world` independent replicas: the steps of all
+    ranks divided by the slowest rank's time.  Returns (value, max time)."""
+    t = dist_max(torch, world, elapsed_s, device)
+    return world * steps_per_rank / t, t
 
 
 # ---------------------------------------------------------------- CPU legs
@@ -353,7 +361,7 @@ def main():
     with ClockSampler(local if world == 1 else 0) as clk:
         el32, launches32 = timed_advance(c32, K, dt, torch)
         dist_barrier(torch, world)
-    el32 = dist_max(torch, world, el32)
+    v32, el32 = replica_throughput(torch, world, K, el32)
     clocks = clk.summary()
 
     # per-pass device times (CUDA events around each launch, separate pass)
@@ -377,13 +385,12 @@ def main():
         K64 = args.fp64_steps or K
         c64.advance(W, R.DT_FIXED, dt)
         el64, l64 = timed_advance(c64, K64, dt, torch)
-        el64 = dist_max(torch, world, el64)
+        v64, el64 = replica_throughput(torch, world, K64, el64)
         ms64, cnt64 = c64.profile_passes(min(K64, 4), dt)
         peak64 = R.fp64_fma_peak()
         flops = fft_flops_per_step(n)
-        v64 = world * K64 / el64
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el64 / K64, "steps": K64,
-                "dtype": "f64", "fp32_speedup": (world * K / el32) / v64,
+                "dtype": "f64", "fp32_speedup": v32 / v64,
                 "roofline": {"bound": "fp64", "achieved": flops * K64 / el64 / 1e12,
                              "peak": peak64, "unit": "TFLOP/s",
                              "frac": flops * K64 / el64 / 1e12 / peak64,
@@ -402,9 +409,9 @@ def main():
         c32.advance(1, R.DT_FIXED, dt)          # H2D dt, launch, D2H time and dt
     a_out, b_out = c32.get_state()              # D2H of the state
     el_e2e = time.perf_counter() - t0
-    el_e2e = dist_max(torch, world, el_e2e)
+    ve2e, el_e2e = replica_throughput(torch, world, e2e_steps, el_e2e)
     S = (n // 2 + 1) * n * 16
-    e2e = {"value": world * e2e_steps / el_e2e, "unit": UNIT,
+    e2e = {"value": ve2e, "unit": UNIT,
            "h2d_bytes_per_step": (2 * S + 8 * e2e_steps) / e2e_steps,
            "d2h_bytes_per_step": (2 * S + 16 * e2e_steps) / e2e_steps,
            "steps": e2e_steps,
@@ -414,7 +421,6 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n, ps, vz, fp, fz)
 
-    v32 = world * K / el32
     line = {"metric": METRIC, "value": v32, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": 1e3 * el32 / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (FP64 reductions)", "data": "synthetic",

@@ -686,7 +686,7 @@ class EngineT final : public IEngine {
   void launch_passA(const cpx<T>* a, const cpx<T>* b) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
-      using C = Cfg<T, N>;
+      using C = Cfg<T, N, PassNT<T, N>::value>;
       auto k = k_passA<T, N>;
       k<<<(gd_.M + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(a, b, tf_, gd_, tw_);
       post("k_passA");
@@ -697,9 +697,10 @@ class EngineT final : public IEngine {
     const T inv4 = (T)(1.0 / ((double)n_ * n_ * n_ * n_));
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
-      using C = Cfg<T, N>;
+      constexpr int NR = PassNT<T, N>::value;
+      using C = Cfg<T, N, NR>;
       auto k = k_passB<T, N, CFL>;
-      k<<<(N + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(tf_, pb_, kxo, gd_, inv4, tw_, enc_);
+      k<<<(N / NR + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(tf_, pb_, kxo, gd_, inv4, tw_, enc_);
       post("k_passB");
     });
   }
@@ -707,7 +708,7 @@ class EngineT final : public IEngine {
                     const StepCoef& sc, int o) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
-      using C = Cfg<T, N>;
+      using C = Cfg<T, N, PassNT<T, N>::value>;
       auto k = k_passC<T, N>;
       k<<<(gd_.M + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(
           pb_, c1in, c2in, planes_[P_PS], planes_[P_VZ], planes_[P_FP], planes_[P_FZ], c1out, c2out, gd_, sc,
@@ -726,10 +727,11 @@ class EngineT final : public IEngine {
       set_smem_attr(k_colfft<T, N, +1>, sm);
       set_smem_attr(k_rowc2r<T, N>, sm);
       set_smem_attr(k_rowr2c<T, N>, sm);
-      set_smem_attr(k_passA<T, N>, sm);
-      set_smem_attr(k_passB<T, N, true>, sm);
-      set_smem_attr(k_passB<T, N, false>, sm);
-      set_smem_attr(k_passC<T, N>, sm);
+      constexpr size_t smp = Cfg<T, N, PassNT<T, N>::value>::SMEM;
+      set_smem_attr(k_passA<T, N>, smp);
+      set_smem_attr(k_passB<T, N, true>, smp);
+      set_smem_attr(k_passB<T, N, false>, smp);
+      set_smem_attr(k_passC<T, N>, smp);
     });
   }
 

@@ -8,7 +8,8 @@
 //
 // The schedule is a Stockham auto-sort: radix-E stages (the last one may have
 // a smaller radix), each an in-register DFT of R points followed by one padded
-// shared-memory exchange.  Twiddles come from a per-N table
+// shared-memory exchange.  NT transforms can be carried at once by the same
+// threads; they share the twiddle loads and the barriers.  Twiddles come from a per-N table
 // tw[k] = exp(-2*pi*i*k/N) built on the host in FP64; the FP32 path stores
 // every twiddle as an (hi, lo) float pair and applies the low part with an
 // extra FMA ("compensated twiddles"), which removes the twiddle rounding from
@@ -128,8 +129,6 @@ template <typename T, int DIR> struct RegDFT<T, 2, DIR> {
   }
 };
 
-__device__ __forceinline__ int spad(int i) { return i + (i >> 5); }
-
 template <int TPF>
 __device__ __forceinline__ void fft_sync() {
   if constexpr (TPF <= 32) {
@@ -139,7 +138,13 @@ __device__ __forceinline__ void fft_sync() {
   }
 }
 
-template <typename T, int N, int E>
+// NT independent length-N transforms carried by the same TPF = N/E threads
+// (thread `lane` holds v[t][q] = x_t[lane + q*TPF]).  The NT transforms share
+// every twiddle load and every barrier.  Shared memory: NT interleaved
+// complex buffers of SMEM_ELEMS elements, padded by one element every
+// 128 bytes so that the strided Stockham writes stay (nearly) bank-conflict
+// free.
+template <typename T, int N, int E, int NT = 1>
 struct BlockFFT {
   static_assert((N & (N - 1)) == 0 && N >= E && E >= 2, "N, E powers of two");
   static constexpr int TPF = N / E;
@@ -147,11 +152,14 @@ struct BlockFFT {
   static constexpr int LOGE = ilog2(E);
   static constexpr int NST = (LOGN + LOGE - 1) / LOGE;
   static constexpr int LAST_R = 1 << (LOGN - LOGE * (NST - 1));
-  static constexpr int SMEM_ELEMS = N + (N >> 5);  // per (re|im) array
-  static constexpr size_t SMEM_BYTES = 2 * SMEM_ELEMS * sizeof(T);
+  static constexpr int PADSH = ilog2(128 / (int)sizeof(cpx<T>));
+  static constexpr int SMEM_ELEMS = N + (N >> PADSH);  // per transform
+  static constexpr size_t SMEM_BYTES = (size_t)NT * SMEM_ELEMS * sizeof(cpx<T>);
+
+  static __device__ __forceinline__ int pad(int i) { return i + (i >> PADSH); }
 
   template <int DIR, int S, int NS>
-  static __device__ __forceinline__ void stage(cpx<T> (&v)[E], int lane, T* sre, T* sim,
+  static __device__ __forceinline__ void stage(cpx<T> (&v)[NT][E], int lane, cpx<T>* sm,
                                                const tw_t<T>* __restrict__ tw) {
     constexpr int R = (S == NST - 1) ? LAST_R : E;
     constexpr int B = E / R;
@@ -160,17 +168,25 @@ struct BlockFFT {
     for (int m = 0; m < B; ++m) {
       const int j = lane + m * TPF;
       const int jm = j & (NS - 1);
-      cpx<T> u[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) u[r] = v[m + r * B];
+      tw_t<T> w[R];
       if constexpr (NS > 1) {
         constexpr int STR = N / (NS * R);
 #pragma unroll
-        for (int r = 1; r < R; ++r) u[r] = twmul<DIR>(u[r], __ldg(&tw[r * jm * STR]));
+        for (int r = 1; r < R; ++r) w[r] = __ldg(&tw[r * jm * STR]);
       }
-      RegDFT<T, R, DIR>::run(u);
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[m + r * B] = u[r];
+      for (int t = 0; t < NT; ++t) {
+        cpx<T> u[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) u[r] = v[t][m + r * B];
+        if constexpr (NS > 1) {
+#pragma unroll
+          for (int r = 1; r < R; ++r) u[r] = twmul<DIR>(u[r], w[r]);
+        }
+        RegDFT<T, R, DIR>::run(u);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[t][m + r * B] = u[r];
+      }
     }
     if constexpr (S < NST - 1) {
 #pragma unroll
@@ -179,42 +195,42 @@ struct BlockFFT {
         const int base = ((j >> LOGNS) << (LOGNS + ilog2(R))) + (j & (NS - 1));
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const int idx = spad(base + r * NS);
-          sre[idx] = v[m + r * B].x;
-          sim[idx] = v[m + r * B].y;
+          const int idx = pad(base + r * NS);
+#pragma unroll
+          for (int t = 0; t < NT; ++t) sm[t * SMEM_ELEMS + idx] = v[t][m + r * B];
         }
       }
       fft_sync<TPF>();
 #pragma unroll
       for (int q = 0; q < E; ++q) {
-        const int idx = spad(lane + q * TPF);
-        v[q] = mkc<T>(sre[idx], sim[idx]);
+        const int idx = pad(lane + q * TPF);
+#pragma unroll
+        for (int t = 0; t < NT; ++t) v[t][q] = sm[t * SMEM_ELEMS + idx];
       }
       fft_sync<TPF>();
-      stage<DIR, S + 1, NS * R>(v, lane, sre, sim, tw);
+      stage<DIR, S + 1, NS * R>(v, lane, sm, tw);
     }
   }
 
-  // X[k] = sum_x x[x] exp(DIR*2*pi*i*x*k/N), unnormalised.
+  // X_t[k] = sum_x x_t[x] exp(DIR*2*pi*i*x*k/N), unnormalised, t < NT.
   template <int DIR>
-  static __device__ __forceinline__ void run(cpx<T> (&v)[E], int lane, T* sre, T* sim,
+  static __device__ __forceinline__ void run(cpx<T> (&v)[NT][E], int lane, cpx<T>* sm,
                                              const tw_t<T>* __restrict__ tw) {
-    stage<DIR, 0, 1>(v, lane, sre, sim, tw);
+    stage<DIR, 0, 1>(v, lane, sm, tw);
   }
 
-  // Write the natural-order result to shared memory so that any thread of
-  // the group can read X[k] and X[N-k] (Hermitian split of packed pairs).
-  static __device__ __forceinline__ void to_smem(const cpx<T> (&v)[E], int lane, T* sre, T* sim) {
+  // Natural-order result to shared memory so that any thread of the group can
+  // read X[k] and X[N-k] (Hermitian split of packed pairs).
+  static __device__ __forceinline__ void to_smem(const cpx<T> (&v)[NT][E], int lane, cpx<T>* sm) {
 #pragma unroll
     for (int q = 0; q < E; ++q) {
-      const int idx = spad(lane + q * TPF);
-      sre[idx] = v[q].x;
-      sim[idx] = v[q].y;
+      const int idx = pad(lane + q * TPF);
+#pragma unroll
+      for (int t = 0; t < NT; ++t) sm[t * SMEM_ELEMS + idx] = v[t][q];
     }
   }
-  static __device__ __forceinline__ cpx<T> from_smem(int k, const T* sre, const T* sim) {
-    const int idx = spad(k);
-    return mkc<T>(sre[idx], sim[idx]);
+  static __device__ __forceinline__ cpx<T> from_smem(int t, int k, const cpx<T>* sm) {
+    return sm[t * SMEM_ELEMS + pad(k)];
   }
 };
 

@@ -39,14 +39,24 @@ struct StepCoef {
   int nn, mm, nnv, mmv;
 };
 
-template <typename T, int N>
+// Launch shape of a kernel carrying NT transforms per thread group: E
+// elements per thread, TPF = N/E threads per transform group, G groups per CTA.
+template <typename T, int N, int NT = 1>
 struct Cfg {
   static constexpr int E = (N >= 8192) ? 16 : 8;
-  using FFT = BlockFFT<T, N, E>;
+  using FFT = BlockFFT<T, N, E, NT>;
   static constexpr int TPF = N / E;
-  static constexpr int G = TPF >= 256 ? 1 : 256 / TPF;  // transforms per CTA
+  static constexpr int G = TPF >= 256 ? 1 : 256 / TPF;  // transform groups per CTA
   static constexpr int THREADS = TPF * G;
   static constexpr size_t SMEM = (size_t)G * FFT::SMEM_BYTES;
+};
+
+// Transforms carried at once by one group in passes A, B and C: two in the
+// FP32 path (shared twiddles and barriers, two rows per 16-byte load in pass
+// B); one in the FP64 path, whose FP64 arithmetic is the bound and whose
+// register budget is already full.
+template <typename T, int N> struct PassNT {
+  static constexpr int value = (sizeof(T) == 4 && N <= 4096) ? 2 : 1;
 };
 
 // ky value of row index j (Rot2D3C.para.f90:220-223)
@@ -80,7 +90,7 @@ __device__ __forceinline__ T powi(T x, int k) {
 
 #define R2D3C_SMEM_DECL                                     \
   extern __shared__ __align__(16) unsigned char smraw_[]; \
-  T* smbase_ = reinterpret_cast<T*>(smraw_);
+  cpx<T>* smbase_ = reinterpret_cast<cpx<T>*>(smraw_);
 
 // --------------------------------------------------------------------------
 // generic y-direction transform of `ncols` contiguous columns of length N
@@ -93,19 +103,18 @@ k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* _
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
-  T* sim = sre + F::SMEM_ELEMS;
+  cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
   const int col = blockIdx.x * C::G + g;
   const bool ok = col < ncols;
   const cpx<T>* src = in + (size_t)(ok ? col : 0) * N;
-  cpx<T> v[C::E];
+  cpx<T> v[1][C::E];
 #pragma unroll
-  for (int q = 0; q < C::E; ++q) v[q] = ok ? src[lane + q * C::TPF] : czero<T>();
-  F::template run<DIR>(v, lane, sre, sim, tw);
+  for (int q = 0; q < C::E; ++q) v[0][q] = ok ? src[lane + q * C::TPF] : czero<T>();
+  F::template run<DIR>(v, lane, sm, tw);
   if (ok) {
     cpx<T>* dst = out + (size_t)col * N;
 #pragma unroll
-    for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[q];
+    for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[0][q];
   }
 }
 
@@ -124,13 +133,12 @@ k_rowc2r(const cpx<T>* __restrict__ tin, T* __restrict__ rout,
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
-  T* sim = sre + F::SMEM_ELEMS;
+  cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
   int pair = blockIdx.x * C::G + g;
   const bool ok = pair < N / 2;
   if (!ok) pair = 0;  // surplus groups recompute pair 0 and store nothing
   const int y0 = 2 * pair;
-  cpx<T> v[C::E];
+  cpx<T> v[1][C::E];
 #pragma unroll
   for (int q = 0; q < C::E; ++q) {
     const int k = lane + q * C::TPF;
@@ -138,28 +146,28 @@ k_rowc2r(const cpx<T>* __restrict__ tin, T* __restrict__ rout,
     const cpx<T> a = tin[(size_t)kk * N + y0];
     const cpx<T> b = tin[(size_t)kk * N + y0 + 1];
     if (k == 0 || k == N / 2) {
-      v[q] = mkc<T>(a.x, b.x);
+      v[0][q] = mkc<T>(a.x, b.x);
     } else if (k < N / 2) {
-      v[q] = mkc<T>(a.x - b.y, a.y + b.x);
+      v[0][q] = mkc<T>(a.x - b.y, a.y + b.x);
     } else {
-      v[q] = mkc<T>(a.x + b.y, b.x - a.y);
+      v[0][q] = mkc<T>(a.x + b.y, b.x - a.y);
     }
   }
-  F::template run<+1>(v, lane, sre, sim, tw);
+  F::template run<+1>(v, lane, sm, tw);
   if (rout && ok) {
 #pragma unroll
     for (int q = 0; q < C::E; ++q) {
       const int x = lane + q * C::TPF;
-      rout[(size_t)y0 * N + x] = v[q].x;
-      rout[(size_t)(y0 + 1) * N + x] = v[q].y;
+      rout[(size_t)y0 * N + x] = v[0][q].x;
+      rout[(size_t)(y0 + 1) * N + x] = v[0][q].y;
     }
   }
   if (mm_enc) {
-    double mx = (double)v[0].x, mn = (double)v[0].x;
+    double mx = (double)v[0][0].x, mn = (double)v[0][0].x;
 #pragma unroll
     for (int q = 0; q < C::E; ++q) {
-      mx = fmax(mx, fmax((double)v[q].x, (double)v[q].y));
-      mn = fmin(mn, fmin((double)v[q].x, (double)v[q].y));
+      mx = fmax(mx, fmax((double)v[0][q].x, (double)v[0][q].y));
+      mn = fmin(mn, fmin((double)v[0][q].x, (double)v[0][q].y));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -185,28 +193,27 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
-  T* sim = sre + F::SMEM_ELEMS;
+  cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
   int pair = blockIdx.x * C::G + g;
   const bool ok = pair < N / 2;
   if (!ok) pair = 0;
   const int y0 = 2 * pair;
-  cpx<T> v[C::E];
+  cpx<T> v[1][C::E];
 #pragma unroll
   for (int q = 0; q < C::E; ++q) {
     const int x = lane + q * C::TPF;
-    v[q] = mkc<T>(rin[(size_t)y0 * N + x], rin[(size_t)(y0 + 1) * N + x]);
+    v[0][q] = mkc<T>(rin[(size_t)y0 * N + x], rin[(size_t)(y0 + 1) * N + x]);
   }
-  F::template run<-1>(v, lane, sre, sim, tw);
-  F::to_smem(v, lane, sre, sim);
+  F::template run<-1>(v, lane, sm, tw);
+  F::to_smem(v, lane, sm);
   fft_sync<C::TPF>();
   const T h = (T)0.5;
 #pragma unroll
   for (int q = 0; q < C::E; ++q) {
     const int k = lane + q * C::TPF;
     if (ok && k <= N / 2) {
-      const cpx<T> w = F::from_smem(k, sre, sim);
-      const cpx<T> u = F::from_smem((N - k) & (N - 1), sre, sim);
+      const cpx<T> w = F::from_smem(0, k, sm);
+      const cpx<T> u = F::from_smem(0, (N - k) & (N - 1), sm);
       tout[(size_t)k * N + y0] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
       tout[(size_t)k * N + y0 + 1] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
     }
@@ -214,18 +221,19 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
 }
 
 // --------------------------------------------------------------------------
-// pass A: masked derivatives + inverse y-FFT, 6 fields per kx column
+// pass A: masked derivatives + inverse y-FFT, 6 fields per kx column, NT
+// fields at a time
 // --------------------------------------------------------------------------
 template <typename T, int N>
-__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+__global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __restrict__ tf,
         DevGrid gd, const tw_t<T>* __restrict__ tw) {
-  using C = Cfg<T, N>;
+  constexpr int NT = PassNT<T, N>::value;
+  using C = Cfg<T, N, NT>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
-  T* sim = sre + F::SMEM_ELEMS;
+  cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
   const int col = blockIdx.x * C::G + g;
   const bool ok = col < gd.M;
   const size_t plane = (size_t)gd.M * N;
@@ -243,105 +251,165 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
     kyv[q] = (T)ky;
     k2v[q] = (T)k2;
   }
-  cpx<T> v[C::E];
+  cpx<T> v[NT][C::E];
 #pragma unroll 1
-  for (int f = 0; f < 6; ++f) {
+  for (int f0 = 0; f0 < 6; f0 += NT) {
 #pragma unroll
-    for (int q = 0; q < C::E; ++q) {
-      // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
-      const T k = (f & 1) ? kyv[q] : kxv;
-      cpx<T> s;
-      if (f < 2) {
-        s = a[q];
-      } else if (f < 4) {
-        const T m = -k2v[q];  // laplak2: -ka2*a
-        s = mkc<T>(m * a[q].x, m * a[q].y);
-      } else {
-        s = b[q];
+    for (int t = 0; t < NT; ++t) {
+      const int f = f0 + t;
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) {
+        // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
+        const T k = (f & 1) ? kyv[q] : kxv;
+        cpx<T> s;
+        if (f < 2) {
+          s = a[q];
+        } else if (f < 4) {
+          const T m = -k2v[q];  // laplak2: -ka2*a
+          s = mkc<T>(m * a[q].x, m * a[q].y);
+        } else {
+          s = b[q];
+        }
+        v[t][q] = mkc<T>(-k * s.y, k * s.x);
       }
-      v[q] = mkc<T>(-k * s.y, k * s.x);
     }
-    F::template run<+1>(v, lane, sre, sim, tw);
+    F::template run<+1>(v, lane, sm, tw);
     if (ok) {
-      cpx<T>* dst = tf + (size_t)f * plane + (size_t)col * N;
 #pragma unroll
-      for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[q];
+      for (int t = 0; t < NT; ++t) {
+        cpx<T>* dst = tf + (size_t)(f0 + t) * plane + (size_t)col * N;
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[t][q];
+      }
     }
   }
 }
 
-// Packed spectrum of a pair of mixed planes (A, B) at row y for x-position k:
-// Z[k] = A[k] + i B[k] on the retained kx < M, conj-extended for k > N - M.
-template <typename T, int N>
-__device__ __forceinline__ cpx<T> packed_pair(const cpx<T>* __restrict__ pa,
-                                              const cpx<T>* __restrict__ pb, int k, int y, int M) {
-  if (k < M) {
-    const cpx<T> a = pa[(size_t)k * N + y];
-    const cpx<T> b = pb[(size_t)k * N + y];
-    if (k == 0) return mkc<T>(a.x, b.x);  // Im of the kx = 0 column is ignored
-    return mkc<T>(a.x - b.y, a.y + b.x);
+// NR consecutive rows y0.. of a mixed plane at column kx: one 16-byte load
+// for two FP32 rows.
+template <typename T, int NR>
+__device__ __forceinline__ void load_rows(const cpx<T>* __restrict__ p, size_t off, cpx<T> (&o)[NR]) {
+  if constexpr (NR == 2 && sizeof(T) == 4) {
+    const float4 w = __ldg(reinterpret_cast<const float4*>(p + off));
+    o[0] = mkc<T>(w.x, w.y);
+    o[1] = mkc<T>(w.z, w.w);
+  } else {
+#pragma unroll
+    for (int t = 0; t < NR; ++t) o[t] = p[off + t];
   }
-  if (k > N - M) {
-    const int kk = N - k;
-    const cpx<T> a = pa[(size_t)kk * N + y];
-    const cpx<T> b = pb[(size_t)kk * N + y];
-    return mkc<T>(a.x + b.y, b.x - a.y);
+}
+
+template <typename T, int NR>
+__device__ __forceinline__ void store_rows(cpx<T>* __restrict__ p, size_t off, const cpx<T> (&o)[NR]) {
+  if constexpr (NR == 2 && sizeof(T) == 4) {
+    *reinterpret_cast<float4*>(p + off) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+  } else {
+#pragma unroll
+    for (int t = 0; t < NR; ++t) p[off + t] = o[t];
   }
-  return czero<T>();
+}
+
+// Packed spectrum of a pair of mixed planes (A, B) at rows y0.. for x-position
+// k: Z[k] = A[k] + i B[k] on the retained kx < M, conj-extended for k > N - M.
+template <typename T, int N, int NR>
+__device__ __forceinline__ void packed_pair(const cpx<T>* __restrict__ pa, const cpx<T>* __restrict__ pb,
+                                            int k, int y0, int M, cpx<T> (&z)[NR]) {
+  if (k < M || k > N - M) {
+    const int kk = k < M ? k : N - k;
+    cpx<T> a[NR], b[NR];
+    load_rows<T, NR>(pa, (size_t)kk * N + y0, a);
+    load_rows<T, NR>(pb, (size_t)kk * N + y0, b);
+#pragma unroll
+    for (int t = 0; t < NR; ++t) {
+      if (k == 0) {
+        z[t] = mkc<T>(a[t].x, b[t].x);  // Im of the kx = 0 column is ignored
+      } else if (k < M) {
+        z[t] = mkc<T>(a[t].x - b[t].y, a[t].y + b[t].x);
+      } else {
+        z[t] = mkc<T>(a[t].x + b[t].y, b[t].x - a[t].y);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < NR; ++t) z[t] = czero<T>();
+  }
 }
 
 // --------------------------------------------------------------------------
-// pass B: per row, the two brackets in physical space and back to mixed space
+// pass B: per group NR rows; the two brackets in physical space and back to
+// mixed space
 // --------------------------------------------------------------------------
 template <typename T, int N, bool CFL>
-__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+__global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
         const tw_t<T>* __restrict__ tw, unsigned long long* __restrict__ cfl_enc) {
-  using C = Cfg<T, N>;
+  constexpr int NR = PassNT<T, N>::value;
+  using C = Cfg<T, N, NR>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
-  T* sim = sre + F::SMEM_ELEMS;
-  int y = blockIdx.x * C::G + g;
-  const bool ok = y < N;
-  if (!ok) y = 0;  // surplus groups recompute row 0 and store nothing
+  cpx<T>* sm = smbase_ + (size_t)g * NR * F::SMEM_ELEMS;
+  int rg = blockIdx.x * C::G + g;
+  const bool ok = rg < N / NR;
+  if (!ok) rg = 0;  // surplus groups recompute rows 0.. and store nothing
+  const int y0 = rg * NR;
   const int M = gd.M;
   const size_t plane = (size_t)M * N;
-  cpx<T> z1[C::E], v[C::E];
-  T p1[C::E];
+  cpx<T> z1[NR][C::E], v[NR][C::E];
+  T p1[NR][C::E];
   // pair (d_x psi, d_y psi)
 #pragma unroll
-  for (int q = 0; q < C::E; ++q) z1[q] = packed_pair<T, N>(tf, tf + plane, lane + q * C::TPF, y, M);
-  F::template run<+1>(z1, lane, sre, sim, tw);
+  for (int q = 0; q < C::E; ++q) {
+    cpx<T> z[NR];
+    packed_pair<T, N, NR>(tf, tf + plane, lane + q * C::TPF, y0, M, z);
+#pragma unroll
+    for (int t = 0; t < NR; ++t) z1[t][q] = z[t];
+  }
+  F::template run<+1>(z1, lane, sm, tw);
   if constexpr (CFL) {
     double m = 0.0;
 #pragma unroll
-    for (int q = 0; q < C::E; ++q) {
-      const double rx = (double)z1[q].x, ry = (double)z1[q].y;
-      m = fmax(m, rx * rx + ry * ry);
-    }
+    for (int t = 0; t < NR; ++t)
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) {
+        const double rx = (double)z1[t][q].x, ry = (double)z1[t][q].y;
+        m = fmax(m, rx * rx + ry * ry);
+      }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(cfl_enc, enc_ordered(m));
   }
   // pair (d_x(-k^2 psi), d_y(-k^2 psi)) -> [psi, -k^2 psi]
 #pragma unroll
-  for (int q = 0; q < C::E; ++q)
-    v[q] = packed_pair<T, N>(tf + 2 * plane, tf + 3 * plane, lane + q * C::TPF, y, M);
-  F::template run<+1>(v, lane, sre, sim, tw);
+  for (int q = 0; q < C::E; ++q) {
+    cpx<T> z[NR];
+    packed_pair<T, N, NR>(tf + 2 * plane, tf + 3 * plane, lane + q * C::TPF, y0, M, z);
 #pragma unroll
-  for (int q = 0; q < C::E; ++q) p1[q] = (z1[q].x * v[q].y - z1[q].y * v[q].x) * inv_n4;
+    for (int t = 0; t < NR; ++t) v[t][q] = z[t];
+  }
+  F::template run<+1>(v, lane, sm, tw);
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < C::E; ++q)
+      p1[t][q] = (z1[t][q].x * v[t][q].y - z1[t][q].y * v[t][q].x) * inv_n4;
   // pair (d_x vz, d_y vz) -> [psi, vz]
 #pragma unroll
-  for (int q = 0; q < C::E; ++q)
-    v[q] = packed_pair<T, N>(tf + 4 * plane, tf + 5 * plane, lane + q * C::TPF, y, M);
-  F::template run<+1>(v, lane, sre, sim, tw);
+  for (int q = 0; q < C::E; ++q) {
+    cpx<T> z[NR];
+    packed_pair<T, N, NR>(tf + 4 * plane, tf + 5 * plane, lane + q * C::TPF, y0, M, z);
 #pragma unroll
-  for (int q = 0; q < C::E; ++q) v[q] = mkc<T>(p1[q], (z1[q].x * v[q].y - z1[q].y * v[q].x) * inv_n4);
+    for (int t = 0; t < NR; ++t) v[t][q] = z[t];
+  }
+  F::template run<+1>(v, lane, sm, tw);
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < C::E; ++q)
+      v[t][q] = mkc<T>(p1[t][q], (z1[t][q].x * v[t][q].y - z1[t][q].y * v[t][q].x) * inv_n4);
   // forward x-FFT of both real products at once
-  F::template run<-1>(v, lane, sre, sim, tw);
-  F::to_smem(v, lane, sre, sim);
+  F::template run<-1>(v, lane, sm, tw);
+  F::to_smem(v, lane, sm);
   fft_sync<C::TPF>();
   const size_t oplane = (size_t)gd.nh * N;
   const T h = (T)0.5;
@@ -349,10 +417,16 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
   for (int q = 0; q < C::E; ++q) {
     const int k = lane + q * C::TPF;
     if (ok && k < kxo) {
-      const cpx<T> w = F::from_smem(k, sre, sim);
-      const cpx<T> u = F::from_smem((N - k) & (N - 1), sre, sim);
-      pb[(size_t)k * N + y] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
-      pb[oplane + (size_t)k * N + y] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+      cpx<T> o1[NR], o2[NR];
+#pragma unroll
+      for (int t = 0; t < NR; ++t) {
+        const cpx<T> w = F::from_smem(t, k, sm);
+        const cpx<T> u = F::from_smem(t, (N - k) & (N - 1), sm);
+        o1[t] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
+        o2[t] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+      }
+      store_rows<T, NR>(pb, (size_t)k * N + y0, o1);
+      store_rows<T, NR>(pb + oplane, (size_t)k * N + y0, o2);
     }
   }
 }
@@ -363,60 +437,83 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
 // last substep c1out/c2out are ps/vz themselves: every element is read and
 // written by the same thread.
 // --------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void rk_update(const cpx<T> c5, const cpx<T> c6, size_t idx, int kyi, int k2,
+                                          const cpx<T>* c1in, const cpx<T>* c2in, const cpx<T>* ps,
+                                          const cpx<T>* vz, const cpx<T>* __restrict__ fp,
+                                          const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out,
+                                          const StepCoef& sc, T tmp1, int kmaxi) {
+  cpx<T> n1 = czero<T>(), n2 = czero<T>();
+  if (k2 <= kmaxi && k2 >= 1) {  // ka2 <= kmax .and. ka2 > tiny (:580)
+    const T nu = (T)sc.nu, hnu = (T)sc.hnu, nuv = (T)sc.nuv, hnuv = (T)sc.hnuv, w2 = (T)sc.w2;
+    const cpx<T> a1 = c1in[idx], a2 = c2in[idx];
+    const T kyf = (T)kyi, ka2 = (T)k2;
+    const cpx<T> C3 = mkc<T>(-kyf * a1.y, kyf * a1.x);  // derivk2(C1,C3,2)
+    const cpx<T> C4 = mkc<T>(-kyf * a2.y, kyf * a2.x);  // derivk2(C2,C4,2)
+    const T tmp2 = (T)1 / ka2;
+    const T tmp3 = (T)1 + (nu * powi(ka2, sc.nn) + hnu * powi(tmp2, sc.mm)) * tmp1;
+    const cpx<T> p0 = ps[idx], f0 = fp[idx];
+    const T u1x = p0.x + ((-c5.x + w2 * C4.x) * tmp2 + f0.x) * tmp1;
+    const T u1y = p0.y + ((-c5.y + w2 * C4.y) * tmp2 + f0.y) * tmp1;
+    n1 = mkc<T>(u1x / tmp3, u1y / tmp3);
+    const T tmp3v = (T)1 + (nuv * powi(ka2, sc.nnv) + hnuv * powi(tmp2, sc.mmv)) * tmp1;
+    const cpx<T> v0 = vz[idx], g0 = fz[idx];
+    const T u2x = v0.x + (c6.x + w2 * C3.x + g0.x) * tmp1;
+    const T u2y = v0.y + (c6.y + w2 * C3.y + g0.y) * tmp1;
+    n2 = mkc<T>(u2x / tmp3v, u2y / tmp3v);
+  }
+  c1out[idx] = n1;
+  c2out[idx] = n2;
+}
+
 template <typename T, int N>
-__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+__global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         const cpx<T>* ps, const cpx<T>* vz, const cpx<T>* __restrict__ fp,
         const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out, DevGrid gd, StepCoef sc,
         const double* __restrict__ dtp, int o, const tw_t<T>* __restrict__ tw) {
-  using C = Cfg<T, N>;
+  constexpr int NT = PassNT<T, N>::value;
+  using C = Cfg<T, N, NT>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  T* sre = smbase_ + (size_t)g * 2 * F::SMEM_ELEMS;
-  T* sim = sre + F::SMEM_ELEMS;
+  cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
   const int col = blockIdx.x * C::G + g;
   const bool ok = col < gd.M;
   const size_t oplane = (size_t)gd.nh * N;
   const cpx<T>* s5 = pb + (size_t)(ok ? col : 0) * N;
-  cpx<T> c5[C::E], c6[C::E];
+  cpx<T> c56[2][C::E];
 #pragma unroll
   for (int q = 0; q < C::E; ++q) {
-    c5[q] = s5[lane + q * C::TPF];
-    c6[q] = s5[oplane + lane + q * C::TPF];
+    c56[0][q] = s5[lane + q * C::TPF];
+    c56[1][q] = s5[oplane + lane + q * C::TPF];
   }
-  F::template run<-1>(c5, lane, sre, sim, tw);
-  F::template run<-1>(c6, lane, sre, sim, tw);
+  if constexpr (NT == 2) {
+    F::template run<-1>(c56, lane, sm, tw);
+  } else {
+    cpx<T> a[1][C::E], b[1][C::E];
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      a[0][q] = c56[0][q];
+      b[0][q] = c56[1][q];
+    }
+    F::template run<-1>(a, lane, sm, tw);
+    F::template run<-1>(b, lane, sm, tw);
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      c56[0][q] = a[0][q];
+      c56[1][q] = b[0][q];
+    }
+  }
   if (!ok) return;
   const T tmp1 = (T)(*dtp / (double)o);  // :581
-  const T nu = (T)sc.nu, hnu = (T)sc.hnu, nuv = (T)sc.nuv, hnuv = (T)sc.hnuv, w2 = (T)sc.w2;
 #pragma unroll
   for (int q = 0; q < C::E; ++q) {
     const int j = lane + q * C::TPF;
     const int ky = ky_of(j, N);
     if (ky > gd.L || -ky > gd.L) continue;
-    const size_t idx = (size_t)col * N + j;
-    const int k2 = col * col + ky * ky;
-    cpx<T> n1 = czero<T>(), n2 = czero<T>();
-    if (k2 <= gd.kmaxi && k2 >= 1) {  // ka2 <= kmax .and. ka2 > tiny (:580)
-      const cpx<T> a1 = c1in[idx], a2 = c2in[idx];
-      const T kyf = (T)ky, ka2 = (T)k2;
-      const cpx<T> C3 = mkc<T>(-kyf * a1.y, kyf * a1.x);  // derivk2(C1,C3,2)
-      const cpx<T> C4 = mkc<T>(-kyf * a2.y, kyf * a2.x);  // derivk2(C2,C4,2)
-      const T tmp2 = (T)1 / ka2;
-      const T tmp3 = (T)1 + (nu * powi(ka2, sc.nn) + hnu * powi(tmp2, sc.mm)) * tmp1;
-      const cpx<T> p0 = ps[idx], f0 = fp[idx];
-      const T u1x = p0.x + ((-c5[q].x + w2 * C4.x) * tmp2 + f0.x) * tmp1;
-      const T u1y = p0.y + ((-c5[q].y + w2 * C4.y) * tmp2 + f0.y) * tmp1;
-      n1 = mkc<T>(u1x / tmp3, u1y / tmp3);
-      const T tmp3v = (T)1 + (nuv * powi(ka2, sc.nnv) + hnuv * powi(tmp2, sc.mmv)) * tmp1;
-      const cpx<T> v0 = vz[idx], g0 = fz[idx];
-      const T u2x = v0.x + (c6[q].x + w2 * C3.x + g0.x) * tmp1;
-      const T u2y = v0.y + (c6[q].y + w2 * C3.y + g0.y) * tmp1;
-      n2 = mkc<T>(u2x / tmp3v, u2y / tmp3v);
-    }
-    c1out[idx] = n1;
-    c2out[idx] = n2;
+    rk_update<T>(c56[0][q], c56[1][q], (size_t)col * N + j, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp, fz,
+                 c1out, c2out, sc, tmp1, gd.kmaxi);
   }
 }
 
