@@ -188,6 +188,17 @@ int r2d3c_inerprod(r2d3c_ctx* ctx, const double* a, const double* b, int kin, do
 /* randu (pseudospec2D_mod.f90:142-161): one draw, *seed updated */
 float r2d3c_randu(int* seed);
 
+/* ---- allocation-free variant ------------------------------------------- */
+/* FP64 complex-to-real 2-D transform on device buffers (same layouts and
+   result as r2d3c_fft_c2r_dev) that performs no device allocation.  No
+   counterpart in the reference.  For callers that cannot allocate device
+   memory (memory owned by another allocator, or no implicit synchronisation
+   allowed); its scratch is a fixed file-scope device array, so n <= 512
+   (larger n returns R2D3C_EINVAL), all calls on a device share that scratch
+   (calls whose GPU work overlaps race), and the first call on each device
+   does the set-up (make it before any stream capture).  stream may be NULL. */
+int r2d3c_fft_c2r_noalloc(int n, const double* d_in, double* d_out, void* stream);
+
 /* ---- measurement ------------------------------------------------------ */
 /* Average device time per launch of the three passes of the RK substep
    (ms_per_launch[0] pass A, [1] pass B, [2] pass C, [3] other kernels) over

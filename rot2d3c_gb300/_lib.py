@@ -71,6 +71,7 @@ SIGNATURES = {
     "r2d3c_fft_c2r": (C.c_int, [_P, _D, _D]),
     "r2d3c_fft_r2c_dev": (C.c_int, [_P, _P, _P, _P]),
     "r2d3c_fft_c2r_dev": (C.c_int, [_P, _P, _P, _P]),
+    "r2d3c_fft_c2r_noalloc": (C.c_int, [C.c_int, _P, _P, _P]),
     "r2d3c_create": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(_P)]),
     "r2d3c_destroy": (C.c_int, [_P]),
     "r2d3c_device_bytes": (C.c_int, [_P, C.POINTER(C.c_longlong)]),

@@ -38,6 +38,15 @@ namespace {
 thread_local std::string g_err;
 void set_err(const std::string& s) { g_err = s; }
 
+}  // namespace
+
+namespace r2d3c {
+// error text slot shared with the entry points defined in other files
+std::string& last_error_slot() { return g_err; }
+}  // namespace r2d3c
+
+namespace {
+
 constexpr double kPi = 3.1415926535897932384;  // module var (pseudospec2D_mod.f90:125)
 
 // randu (pseudospec2D_mod.f90:142-161): XOR-masked Park-Miller step with
