@@ -29,6 +29,7 @@ import statistics
 import subprocess
 import sys
 import time
+import time as time_mod
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -50,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--err-steps", type=int, default=100)
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--ensemble-steps", type=int, default=500)
     return ap.parse_args()
 
 
@@ -249,6 +252,93 @@ def replica_throughput(torch, world, steps_per_rank, elapsed_s, device="cuda"):
     return world * steps_per_rank / t, t
 
 
+# ---------------------------------------------------------------- ensemble
+ENSEMBLE = dict(groups=((512, 64), (1024, 16), (2048, 4)), omega_lo=0.1, omega_hi=100.0, hnu=0.1,
+                cfl=0.5, ic_kmin=1.0, ic_kmax=10.0, f_kmin=4.0, f_kmax=6.0, seed=7)
+
+
+def ensemble_inputs():
+    """Per-run (n, params dict, ps, vz, fp, fz) of the batched ensemble:
+    Omega log-uniform in [0.1, 100], nu = 1e-3 (256/n)^2, independent IC and
+    forcing seeds; IC |u| ~ k^-1 on 1 <= |k| <= 10 with energy 0.5 per field,
+    forcing shell 4-6 normalised like iflow = 1."""
+    import numpy as np
+    e = ENSEMBLE
+    rng = np.random.default_rng(e["seed"])
+    runs = []
+    seed = 1000
+    for n, count in e["groups"]:
+        for _ in range(count):
+            om = float(np.exp(rng.uniform(np.log(e["omega_lo"]), np.log(e["omega_hi"]))))
+            nu = 1e-3 * (256.0 / n) ** 2
+            ps, ka2 = synthetic_field(n, e["ic_kmin"], e["ic_kmax"], -2.0, seed)
+            vz, _ = synthetic_field(n, e["ic_kmin"], e["ic_kmax"], -1.0, seed + 1)
+            fp, _ = synthetic_field(n, e["f_kmin"], e["f_kmax"], 0.0, seed + 2)
+            fz, _ = synthetic_field(n, e["f_kmin"], e["f_kmax"], 0.0, seed + 3)
+            seed += 4
+            ps *= math.sqrt(0.5 / _energy(ps, ka2, 1, n))
+            vz *= math.sqrt(0.5 / _energy(vz, ka2, 0, n))
+            fp *= math.sqrt(1.0 / _energy(fp, ka2, 1, n))
+            fz *= math.sqrt(1.0 / _energy(fz, ka2, 0, n))
+            prm = dict(n=n, nu=nu, nuv=nu, hnu=e["hnu"], hnuv=e["hnu"], nn=1, mm=2, nnv=1, mmv=2, omega=om,
+                       iflow=0, cfl=e["cfl"], kup=e["f_kmax"], kdn=e["f_kmin"])
+            runs.append((n, prm, ps, vz, fp, fz))
+    return runs
+
+
+def run_ensemble(args, torch):
+    """runs/s of the batched ensemble (all runs advance `steps` CFL steps in
+    one CUDA graph per step) and each run's total-energy budget residual
+    (BalanceTest_Rot2D3C.py: d/dt (E + Ez)/2 = inj - diss) over 100 steps."""
+    import numpy as np
+    import rot2d3c_gb300 as R
+    runs = ensemble_inputs()
+    groups = []
+    for n, count in ENSEMBLE["groups"]:
+        groups.append((n, [R.make_params(**r[1]) for r in runs if r[0] == n]))
+    ens = R.Ensemble(groups, R.FP32)
+    for i, (n, prm, ps, vz, fp, fz) in enumerate(runs):
+        ens.set_state(i, ps, vz)
+        ens.set_forcing(i, fp, fz)
+        ens.set_time(i, 0.0)
+    # budget: cond_check every 10 steps over 100 steps (outside the timed region)
+    samples = []
+    t = np.zeros(len(runs))
+    for k in range(11):
+        samples.append(np.array([ens.cond_check(i, t[i]) for i in range(len(runs))]))
+        if k < 10:
+            t = ens.advance(10, R.DT_CFL, ENSEMBLE["cfl"])
+    S = np.array(samples)  # [sample][run][30]
+    time = S[:, :, 0]
+    etot = 0.5 * (S[:, :, 1] + S[:, :, 2])
+    inj = S[:, :, 3] + S[:, :, 4]
+    diss = S[:, :, 5] + S[:, :, 6] + S[:, :, 7] + S[:, :, 8]
+    resid = []
+    for i in range(len(runs)):
+        dE = np.gradient(etot[:, i], time[:, i])
+        r = dE - (inj[:, i] - diss[:, i])
+        resid.append(float(np.abs(np.mean(r[1:-1])) / max(np.mean(np.abs(inj[:, i])), 1e-300)))
+    resid = np.array(resid)
+    # timed: `steps` more steps of every run
+    K = args.ensemble_steps
+    ens.advance(3, R.DT_CFL, ENSEMBLE["cfl"])  # warm-up
+    l0 = ens.kernel_launches()
+    torch.cuda.synchronize()
+    t0 = time_mod.perf_counter()
+    ens.advance(K, R.DT_CFL, ENSEMBLE["cfl"])
+    el = time_mod.perf_counter() - t0
+    out = {"value": len(runs) / el, "unit": f"runs/s ({K} RK4 steps per run)",
+           "runs": len(runs), "groups": [list(g) for g in ENSEMBLE["groups"]], "steps_per_run": K,
+           "seconds": el, "gpu_launches": ens.kernel_launches() - l0, "dtype": "f32 (FP64 reductions)",
+           "budget_residual": {"median": float(np.median(resid)), "max": float(resid.max()),
+                               "definition": "|mean(dE_tot/dt - (inj - diss))| / mean|inj| over 100 steps, "
+                                             "cond_check every 10 steps"},
+           "config": "64 x 512^2 + 16 x 1024^2 + 4 x 2048^2, Omega log-uniform [0.1,100], nu=1e-3(256/n)^2, "
+                     "hnu=0.1, CFL=0.5, forcing shell 4-6, independent seeds"}
+    ens.destroy()
+    return out
+
+
 # ---------------------------------------------------------------- CPU legs
 def cpu_baseline(n, ps, vz, fp, fz, budget_s=20.0):
     """The C/OpenMP restatement of the reference step (oracle/cpu) on all host
@@ -417,6 +507,8 @@ def main():
            "steps": e2e_steps,
            "path": "r2d3c_set_state + per-step r2d3c_advance(1) + r2d3c_get_state (host FP64 buffers)"}
 
+    ensemble = None if args.no_ensemble else run_ensemble(args, torch)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n, ps, vz, fp, fz)
@@ -430,7 +522,7 @@ def main():
                        "l2": "working set larger than L2 (6 mixed planes of 268 MB at 4096^2 FP32)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches32, "roofline": roofline, "clocks": clocks, "e2e": e2e,
-            "fp64": fp64, "cpu_baseline": cpu}
+            "fp64": fp64, "ensemble": ensemble, "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
     c32.destroy()

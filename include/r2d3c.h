@@ -172,6 +172,32 @@ int r2d3c_transfers(r2d3c_ctx* ctx, double* Fl0, double* Fl1, double* Fl2);
    scaled by 1/n^2 before the C2R, as R(n,n). */
 int r2d3c_get_field(r2d3c_ctx* ctx, int which, double* R);
 
+/* ---- Ensembles of independent runs ------------------------------------- */
+/* No counterpart in the reference (it runs one field per MPI job).  Several
+   runs of possibly different sizes advance together: runs of the same n are
+   batched into the same kernel launches (one CTA row per run), and one step
+   of every size group is captured in one CUDA graph with the groups on
+   parallel streams.  Each run has its own parameters (n, nu, Omega, ...),
+   state, forcing (held constant, iflow 0/1 semantics), dt and time.  Runs
+   are numbered group by group in the order given. */
+typedef struct r2d3c_ensemble r2d3c_ensemble;
+/* ngroups size groups; group g has runs[g] runs of grid n[g]; params holds
+   one r2d3c_params per run (params[r].n must equal its group's n). */
+int r2d3c_ensemble_create(int ngroups, const int* n, const int* runs, const r2d3c_params* params,
+                          int precision, r2d3c_ensemble** ens);
+int r2d3c_ensemble_destroy(r2d3c_ensemble* ens);
+int r2d3c_ensemble_set_state(r2d3c_ensemble* ens, int run, const double* ps_hat, const double* vz_hat);
+int r2d3c_ensemble_get_state(r2d3c_ensemble* ens, int run, double* ps_hat, double* vz_hat);
+int r2d3c_ensemble_set_forcing(r2d3c_ensemble* ens, int run, const double* fp_hat, const double* fz_hat);
+/* nsteps steps of every run (dt per run from its CFL condition, or fixed);
+   times (may be NULL) receives each run's time. */
+int r2d3c_ensemble_advance(r2d3c_ensemble* ens, int nsteps, int dt_mode, double cfl_or_dt, double* times);
+int r2d3c_ensemble_set_time(r2d3c_ensemble* ens, int run, double time);
+/* cond_check / spectrum of one run (as r2d3c_cond_check, r2d3c_spectrum) */
+int r2d3c_ensemble_cond_check(r2d3c_ensemble* ens, int run, double time, double out[30]);
+int r2d3c_ensemble_spectrum(r2d3c_ensemble* ens, int run, double* Ek, double* Ezk);
+int r2d3c_ensemble_kernel_launches(const r2d3c_ensemble* ens, long long* count);
+
 /* ---- Level 2 operators (reference subroutines on host arrays) ---------- */
 /* derivk2 (pseudospec2D_Rot2D3C.f90:6-68) */
 int r2d3c_derivk2(r2d3c_ctx* ctx, const double* a, double* b, int dir);

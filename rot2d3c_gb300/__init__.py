@@ -30,7 +30,7 @@ __all__ = [
     "FP64", "FP32", "R2C", "C2R", "DT_CFL", "DT_FIXED", "FIELD_PS", "FIELD_VZ", "FIELD_WW",
     "FIELD_INVLAP_PSI", "Params", "R2D3CError", "FFTPlan", "Context", "randu", "load",
     "fftp2d_create_plan", "fftp2d_real_to_complex", "fftp2d_complex_to_real",
-    "fftp2d_destroy_plan", "make_params",
+    "fftp2d_destroy_plan", "make_params", "Ensemble",
 ]
 
 _DP = C.POINTER(C.c_double)
@@ -321,6 +321,77 @@ class Context:
     def destroy(self) -> None:
         if getattr(self, "_h", None):
             load().r2d3c_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Ensemble:
+    """Independent runs advanced together (r2d3c_ensemble_*): runs of equal n
+    share kernel launches, and one CUDA graph holds one step of every size
+    group.  ``groups`` is a list of (n, [Params, ...]); runs are numbered
+    group by group."""
+
+    def __init__(self, groups, precision: int = FP64):
+        ns = [int(n) for n, _ in groups]
+        runs = [len(ps) for _, ps in groups]
+        allp = [p for _, ps in groups for p in ps]
+        self.ns = [n for n, ps in groups for _ in ps]
+        arr = (Params * len(allp))(*allp)
+        h = C.c_void_p()
+        check(load().r2d3c_ensemble_create(len(groups), (C.c_int * len(ns))(*ns), (C.c_int * len(runs))(*runs),
+                                           arr, precision, C.byref(h)), "ensemble_create")
+        self._h = h
+        self.nruns = len(allp)
+
+    def set_state(self, run: int, ps, vz) -> None:
+        n = self.ns[run]
+        a, b = _spec_in(ps, n), _spec_in(vz, n)
+        check(load().r2d3c_ensemble_set_state(self._h, run, _dptr(a), _dptr(b)), "ensemble_set_state")
+
+    def get_state(self, run: int):
+        n = self.ns[run]
+        a = np.empty((n // 2 + 1, n), np.complex128)
+        b = np.empty_like(a)
+        check(load().r2d3c_ensemble_get_state(self._h, run, _dptr(a), _dptr(b)), "ensemble_get_state")
+        return a, b
+
+    def set_forcing(self, run: int, fp, fz) -> None:
+        n = self.ns[run]
+        a, b = _spec_in(fp, n), _spec_in(fz, n)
+        check(load().r2d3c_ensemble_set_forcing(self._h, run, _dptr(a), _dptr(b)), "ensemble_set_forcing")
+
+    def set_time(self, run: int, t: float) -> None:
+        check(load().r2d3c_ensemble_set_time(self._h, run, t), "ensemble_set_time")
+
+    def advance(self, nsteps: int, dt_mode: int, cfl_or_dt: float) -> np.ndarray:
+        t = np.empty(self.nruns)
+        check(load().r2d3c_ensemble_advance(self._h, nsteps, dt_mode, cfl_or_dt, _dptr(t)), "ensemble_advance")
+        return t
+
+    def cond_check(self, run: int, time: float) -> np.ndarray:
+        out = np.empty(30)
+        check(load().r2d3c_ensemble_cond_check(self._h, run, time, _dptr(out)), "ensemble_cond_check")
+        return out
+
+    def spectrum(self, run: int):
+        nb = self.ns[run] // 2 + 1
+        ek, ezk = np.empty(nb), np.empty(nb)
+        check(load().r2d3c_ensemble_spectrum(self._h, run, _dptr(ek), _dptr(ezk)), "ensemble_spectrum")
+        return ek, ezk
+
+    def kernel_launches(self) -> int:
+        c = C.c_longlong()
+        check(load().r2d3c_ensemble_kernel_launches(self._h, C.byref(c)), "ensemble_kernel_launches")
+        return c.value
+
+    def destroy(self) -> None:
+        if getattr(self, "_h", None):
+            load().r2d3c_ensemble_destroy(self._h)
             self._h = None
 
     def __del__(self):

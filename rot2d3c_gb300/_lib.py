@@ -91,6 +91,16 @@ SIGNATURES = {
     "r2d3c_spectrum": (C.c_int, [_P, _D, _D]),
     "r2d3c_transfers": (C.c_int, [_P, _D, _D, _D]),
     "r2d3c_get_field": (C.c_int, [_P, C.c_int, _D]),
+    "r2d3c_ensemble_create": (C.c_int, [C.c_int, _I, _I, C.POINTER(Params), C.c_int, C.POINTER(_P)]),
+    "r2d3c_ensemble_destroy": (C.c_int, [_P]),
+    "r2d3c_ensemble_set_state": (C.c_int, [_P, C.c_int, _D, _D]),
+    "r2d3c_ensemble_get_state": (C.c_int, [_P, C.c_int, _D, _D]),
+    "r2d3c_ensemble_set_forcing": (C.c_int, [_P, C.c_int, _D, _D]),
+    "r2d3c_ensemble_advance": (C.c_int, [_P, C.c_int, C.c_int, C.c_double, _D]),
+    "r2d3c_ensemble_set_time": (C.c_int, [_P, C.c_int, C.c_double]),
+    "r2d3c_ensemble_cond_check": (C.c_int, [_P, C.c_int, C.c_double, _D]),
+    "r2d3c_ensemble_spectrum": (C.c_int, [_P, C.c_int, _D, _D]),
+    "r2d3c_ensemble_kernel_launches": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "r2d3c_derivk2": (C.c_int, [_P, _D, _D, C.c_int]),
     "r2d3c_laplak2": (C.c_int, [_P, _D, _D]),
     "r2d3c_inv_laplak2": (C.c_int, [_P, _D, _D]),

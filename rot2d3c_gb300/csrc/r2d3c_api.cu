@@ -94,6 +94,37 @@ struct r2d3c_plan {
   std::unique_ptr<IEngine> eng;
 };
 
+struct r2d3c_ensemble {
+  struct Group {
+    int n = 0, runs = 0, first = 0;
+    std::unique_ptr<IEngine> eng;
+  };
+  std::vector<Group> groups;
+  std::vector<r2d3c_params> params;
+  cudaStream_t master = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t graph = nullptr;
+  int graph_cfl = -1;
+  long long graph_launches = 0, launches = 0;
+  ~r2d3c_ensemble() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (cudaEvent_t e : joins) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (master) cudaStreamDestroy(master);
+  }
+  // (group, local run) of a global run index
+  Group& locate(int run, int* local) {
+    for (Group& g : groups)
+      if (run >= g.first && run < g.first + g.runs) {
+        *local = run - g.first;
+        g.eng->select_run(*local);
+        return g;
+      }
+    throw r2d3c::Error(r2d3c::kEINVAL, "run index out of range");
+  }
+};
+
 #define API_BEGIN try {
 #define API_END                                                  \
   }                                                              \
@@ -605,6 +636,190 @@ int r2d3c_get_field(r2d3c_ctx* ctx, int which, double* R) {
   }
   e->c2r(P_W1, R_1, nullptr, nullptr);
   e->download_real(R_1, R);
+  API_END
+}
+
+// ---------------------------------------------------------------- ensembles
+int r2d3c_ensemble_create(int ngroups, const int* n, const int* runs, const r2d3c_params* params,
+                          int precision, r2d3c_ensemble** ens) {
+  API_BEGIN
+  REQUIRE(ens && n && runs && params, "NULL argument");
+  *ens = nullptr;
+  REQUIRE(ngroups >= 1 && ngroups <= 16, "ngroups must be 1..16");
+  REQUIRE(precision == R2D3C_FP64 || precision == R2D3C_FP32, "bad precision");
+  std::unique_ptr<r2d3c_ensemble> e(new r2d3c_ensemble());
+  int total = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    REQUIRE(supported_n(n[g]), "n must be a power of two in [16, 8192]");
+    REQUIRE(runs[g] >= 1 && runs[g] <= 4096, "runs per group must be 1..4096");
+    total += runs[g];
+  }
+  e->params.assign(params, params + total);
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  int first = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    std::vector<ModelCoef> mc;
+    for (int r = first; r < first + runs[g]; ++r) {
+      const r2d3c_params& p = e->params[r];
+      check_params(&p);
+      REQUIRE(p.n == n[g], "params[r].n differs from its group's n");
+      REQUIRE(p.iflow == 0 || p.iflow == 1, "ensemble runs hold their forcing constant (iflow 0 or 1)");
+      mc.push_back(ModelCoef{p.nu, p.hnu, p.nuv, p.hnuv, p.omega, p.nn, p.mm, p.nnv, p.mmv});
+    }
+    r2d3c_ensemble::Group gr;
+    gr.n = n[g];
+    gr.runs = runs[g];
+    gr.first = first;
+    gr.eng.reset(precision == R2D3C_FP64 ? make_engine_f64(n[g], dev, true, runs[g])
+                                         : make_engine_f32(n[g], dev, true, runs[g]));
+    gr.eng->set_run_coefs(mc);
+    e->groups.push_back(std::move(gr));
+    first += runs[g];
+  }
+  cuda_check(cudaStreamCreateWithFlags(&e->master, cudaStreamNonBlocking), "cudaStreamCreate");
+  cuda_check(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming), "cudaEventCreate");
+  e->joins.resize(ngroups);
+  for (auto& j : e->joins) cuda_check(cudaEventCreateWithFlags(&j, cudaEventDisableTiming), "cudaEventCreate");
+  *ens = e.release();
+  API_END
+}
+
+int r2d3c_ensemble_destroy(r2d3c_ensemble* ens) {
+  API_BEGIN
+  delete ens;
+  API_END
+}
+
+int r2d3c_ensemble_set_state(r2d3c_ensemble* ens, int run, const double* ps_hat, const double* vz_hat) {
+  API_BEGIN
+  REQUIRE(ens && ps_hat && vz_hat, "NULL argument");
+  int l = 0;
+  auto& g = ens->locate(run, &l);
+  g.eng->upload_spec(P_PS, ps_hat);
+  g.eng->upload_spec(P_VZ, vz_hat);
+  g.eng->mark_state_untruncated();
+  API_END
+}
+
+int r2d3c_ensemble_get_state(r2d3c_ensemble* ens, int run, double* ps_hat, double* vz_hat) {
+  API_BEGIN
+  REQUIRE(ens, "NULL argument");
+  int l = 0;
+  auto& g = ens->locate(run, &l);
+  if (ps_hat) g.eng->download_spec(P_PS, ps_hat);
+  if (vz_hat) g.eng->download_spec(P_VZ, vz_hat);
+  API_END
+}
+
+int r2d3c_ensemble_set_forcing(r2d3c_ensemble* ens, int run, const double* fp_hat, const double* fz_hat) {
+  API_BEGIN
+  REQUIRE(ens && fp_hat && fz_hat, "NULL argument");
+  int l = 0;
+  auto& g = ens->locate(run, &l);
+  g.eng->upload_spec(P_FP, fp_hat);
+  g.eng->upload_spec(P_FZ, fz_hat);
+  API_END
+}
+
+int r2d3c_ensemble_set_time(r2d3c_ensemble* ens, int run, double time) {
+  API_BEGIN
+  REQUIRE(ens, "NULL argument");
+  int l = 0;
+  auto& g = ens->locate(run, &l);
+  g.eng->set_time(time);
+  API_END
+}
+
+int r2d3c_ensemble_advance(r2d3c_ensemble* ens, int nsteps, int dt_mode, double cfl_or_dt, double* times) {
+  API_BEGIN
+  REQUIRE(ens, "NULL argument");
+  REQUIRE(nsteps >= 0, "nsteps must be >= 0");
+  REQUIRE(dt_mode == R2D3C_DT_CFL || dt_mode == R2D3C_DT_FIXED, "bad dt_mode");
+  REQUIRE(cfl_or_dt > 0.0 && std::isfinite(cfl_or_dt), "cfl_or_dt must be positive and finite");
+  const bool cfl = dt_mode == R2D3C_DT_CFL;
+  for (auto& g : ens->groups) {
+    if (!cfl) g.eng->set_dt_all(cfl_or_dt);
+    g.eng->prepare_steps(cfl ? cfl_or_dt : 0.0);
+  }
+  if (!ens->graph || ens->graph_cfl != (int)cfl) {
+    if (ens->graph) cudaGraphExecDestroy(ens->graph);
+    ens->graph = nullptr;
+    // one step of every group, the groups forked onto their own streams
+    long long before = 0;
+    for (auto& g : ens->groups) before += g.eng->kernel_launches();
+    cudaGraph_t graph = nullptr;
+    cuda_check(cudaStreamBeginCapture(ens->master, cudaStreamCaptureModeThreadLocal), "BeginCapture");
+    try {
+      cuda_check(cudaEventRecord(ens->fork, ens->master), "cudaEventRecord");
+      for (size_t i = 0; i < ens->groups.size(); ++i) {
+        IEngine* eng = ens->groups[i].eng.get();
+        cuda_check(cudaStreamWaitEvent(eng->stream(), ens->fork, 0), "cudaStreamWaitEvent");
+        eng->enqueue_steps(cfl);
+        cuda_check(cudaEventRecord(ens->joins[i], eng->stream()), "cudaEventRecord");
+        cuda_check(cudaStreamWaitEvent(ens->master, ens->joins[i], 0), "cudaStreamWaitEvent");
+      }
+    } catch (...) {
+      cudaStreamEndCapture(ens->master, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    cuda_check(cudaStreamEndCapture(ens->master, &graph), "EndCapture");
+    const cudaError_t ie = cudaGraphInstantiate(&ens->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    cuda_check(ie, "GraphInstantiate");
+    long long after = 0;
+    for (auto& g : ens->groups) after += g.eng->kernel_launches();
+    ens->graph_launches = after - before;
+    ens->graph_cfl = (int)cfl;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    cuda_check(cudaGraphLaunch(ens->graph, ens->master), "GraphLaunch");
+    ens->launches += ens->graph_launches;
+  }
+  cuda_check(cudaStreamSynchronize(ens->master), "cudaStreamSynchronize");
+  if (times) {
+    for (auto& g : ens->groups) {
+      std::vector<double> t(g.runs);
+      g.eng->get_scalars(nullptr, t.data());
+      for (int r = 0; r < g.runs; ++r) times[g.first + r] = t[r];
+    }
+  }
+  API_END
+}
+
+int r2d3c_ensemble_cond_check(r2d3c_ensemble* ens, int run, double time, double out[30]) {
+  API_BEGIN
+  REQUIRE(ens && out, "NULL argument");
+  int l = 0;
+  auto& g = ens->locate(run, &l);
+  r2d3c_ctx view;
+  view.p = ens->params[run];
+  view.eng.reset(g.eng.get());
+  const int rc = r2d3c_cond_check(&view, time, out);
+  view.eng.release();
+  if (rc != R2D3C_OK) return rc;
+  API_END
+}
+
+int r2d3c_ensemble_spectrum(r2d3c_ensemble* ens, int run, double* Ek, double* Ezk) {
+  API_BEGIN
+  REQUIRE(ens && Ek && Ezk, "NULL argument");
+  int l = 0;
+  auto& g = ens->locate(run, &l);
+  r2d3c_ctx view;
+  view.p = ens->params[run];
+  view.eng.reset(g.eng.get());
+  const int rc = r2d3c_spectrum(&view, Ek, Ezk);
+  view.eng.release();
+  if (rc != R2D3C_OK) return rc;
+  API_END
+}
+
+int r2d3c_ensemble_kernel_launches(const r2d3c_ensemble* ens, long long* count) {
+  API_BEGIN
+  REQUIRE(ens && count, "NULL argument");
+  *count = ens->launches;
   API_END
 }
 

@@ -293,8 +293,14 @@ __device__ __forceinline__ double dec_ordered(unsigned long long e) {
   return __longlong_as_double((long long)b);
 }
 
-static __global__ void k_cfl_dt(const unsigned long long* __restrict__ enc, CflCoef c, double* scal,
-                         int add_time) {
+// one thread per run r: enc, scal at r * kScalStride, coefficients c[r]
+static __global__ void k_cfl_dt(const unsigned long long* __restrict__ enc, const CflCoef* __restrict__ cc,
+                                double* scal, int add_time, int nruns) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nruns) return;
+  enc += r * kScalStride;
+  scal += r * kScalStride;
+  const CflCoef c = cc[r];
   const double m = dec_ordered(enc[0]);
   const double tmp = __ddiv_rn(sqrt(m), c.nrm);
   const double den = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(c.kcut, tmp), c.nuk), c.nuvk), c.w2);
@@ -303,7 +309,10 @@ static __global__ void k_cfl_dt(const unsigned long long* __restrict__ enc, CflC
   if (add_time) scal[1] = __dadd_rn(scal[1], dt);
 }
 
-static __global__ void k_add_time(double* scal) { scal[1] = __dadd_rn(scal[1], scal[0]); }
+static __global__ void k_add_time(double* scal, int nruns) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nruns) scal[r * kScalStride + 1] = __dadd_rn(scal[r * kScalStride + 1], scal[r * kScalStride]);
+}
 
 // ---------------------------------------------------------------------------
 // rand_force (pseudospec2D_Rot2D3C.f90:1063-1126): the plane is zero except

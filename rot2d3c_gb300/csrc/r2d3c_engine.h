@@ -85,6 +85,19 @@ class IEngine {
   virtual double get_dt() = 0;
   virtual double get_time() = 0;
   virtual void mark_state_untruncated() = 0;
+  // Batched engines hold nruns() runs of the same n that advance together;
+  // per-run operations (state, forcing, diagnostics, dt, time) act on the run
+  // chosen by select_run.  Each run has its own coefficients.
+  virtual int nruns() const = 0;
+  virtual void select_run(int r) = 0;
+  virtual void set_run_coefs(const std::vector<ModelCoef>& mc) = 0;
+  virtual void set_dt_all(double dt) = 0;
+  virtual void get_scalars(double* dt, double* time) = 0;  // per run
+  // Two-phase step for capture into an outer CUDA graph: prepare (uploads,
+  // truncation; synchronises) before the capture, then enqueue one step of
+  // every run on stream() while the capture is open.
+  virtual void prepare_steps(double cfl) = 0;
+  virtual void enqueue_steps(bool cfl_mode) = 0;
   virtual void rand_force(const RandForceHost f[2]) = 0;
   // One RK4 step.  cfl_mode: dt from the CFL condition of the current state
   // (fused into the first substep), else the dt already set.  add_time:
@@ -113,9 +126,10 @@ class IEngine {
   virtual void profile_steps(const ModelCoef& mc, int nsteps, double ms[4], long long cnt[4]) = 0;
 };
 
-// full = false allocates only what the Level-1 transforms need.
-IEngine* make_engine_f64(int n, int device, bool full);
-IEngine* make_engine_f32(int n, int device, bool full);
+// full = false allocates only what the Level-1 transforms need; nb > 1 makes
+// a batched engine of nb runs.
+IEngine* make_engine_f64(int n, int device, bool full, int nb = 1);
+IEngine* make_engine_f32(int n, int device, bool full, int nb = 1);
 bool supported_n(int n);
 
 }  // namespace r2d3c

@@ -3,5 +3,7 @@
 #include "r2d3c_engine_impl.cuh"
 
 namespace r2d3c {
-IEngine* make_engine_f32(int n, int device, bool full) { return new EngineT<float>(n, device, full); }
+IEngine* make_engine_f32(int n, int device, bool full, int nb) {
+  return new EngineT<float>(n, device, full, nb);
+}
 }  // namespace r2d3c

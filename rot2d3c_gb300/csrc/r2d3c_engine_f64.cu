@@ -2,5 +2,7 @@
 #include "r2d3c_engine_impl.cuh"
 
 namespace r2d3c {
-IEngine* make_engine_f64(int n, int device, bool full) { return new EngineT<double>(n, device, full); }
+IEngine* make_engine_f64(int n, int device, bool full, int nb) {
+  return new EngineT<double>(n, device, full, nb);
+}
 }  // namespace r2d3c

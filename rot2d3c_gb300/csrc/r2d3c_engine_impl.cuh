@@ -73,7 +73,8 @@ __global__ void k_randforce_seq(cpx<T>* fp, cpx<T>* fz, const double* __restrict
 template <typename T>
 class EngineT final : public IEngine {
  public:
-  EngineT(int n, int device, bool full) : n_(n), dev_(device), full_(full) {
+  EngineT(int n, int device, bool full, int nb = 1) : n_(n), dev_(device), full_(full), nb_(nb) {
+    if (nb < 1 || (nb > 1 && !full)) throw Error(kEINVAL, "bad batch size");
     if (!supported_n(n)) throw Error(kEINVAL, "unsupported grid size n");
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     cuda_check(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -86,26 +87,31 @@ class EngineT final : public IEngine {
     S_ = (size_t)gd_.nh * n;
     try {
       for (int p = 0; p < P_COUNT; ++p)
-        if (full || p == P_W1) planes_[p] = alloc<cpx<T>>(S_);
+        if (full || p == P_W1) pbase_[p] = planes_[p] = alloc<cpx<T>>(S_ * (batched(p) ? nb_ : 1));
       for (int r = 0; r < R_COUNT; ++r)
         if (full || r == R_1) rplanes_[r] = alloc<T>((size_t)n * n);
       if (full) {
-        tf_ = alloc<cpx<T>>((size_t)6 * gd_.M * n);
-        pb_ = alloc<cpx<T>>(2 * S_);
+        tf_ = alloc<cpx<T>>((size_t)6 * gd_.M * n * nb_);
+        pb_ = alloc<cpx<T>>(2 * S_ * nb_);
       }
       tg_ = alloc<cpx<T>>(S_);
       tw_ = alloc<tw_t<T>>((size_t)n);
       stage_count_ = std::max(2 * S_, (size_t)n * n);
       if (!std::is_same<T, double>::value) stage64_ = alloc<double>(stage_count_);
-      scal_ = alloc<double>(8);
-      enc_ = alloc<unsigned long long>(8);
+      scal_base_ = scal_ = alloc<double>((size_t)kScalStride * nb_);
+      enc_base_ = enc_ = alloc<unsigned long long>((size_t)kScalStride * nb_);
+      d_sc_ = alloc<StepCoef>(nb_);
+      d_cfl_ = alloc<CflCoef>(nb_);
+      dirty_.assign(nb_, 0);
       partials_ = alloc<double>((size_t)kSumBlocks * kMaxTerms);
       small_ = alloc<double>((size_t)kMaxTerms + 5 * (size_t)gd_.nh);
       cuda_check(cudaMallocHost(&hsmall_, sizeof(double) * (kMaxTerms + 5 * (size_t)gd_.nh + 16)),
                  "cudaMallocHost");
-      cuda_check(cudaMemsetAsync(scal_, 0, 8 * sizeof(double), st_), "memset");
+      cuda_check(cudaMemsetAsync(scal_base_, 0, kScalStride * nb_ * sizeof(double), st_), "memset");
       for (int p = 0; p < P_COUNT; ++p)
-        if (planes_[p]) zero_spec(p);
+        if (pbase_[p])
+          cuda_check(cudaMemsetAsync(pbase_[p], 0, S_ * (batched(p) ? nb_ : 1) * sizeof(cpx<T>), st_),
+                     "memset plane");
       build_twiddles();
       set_kernel_attrs();
       sync();
@@ -308,10 +314,10 @@ class EngineT final : public IEngine {
   }
   void brackets_full() {
     // [psi, -k^2 psi] -> B5 and [psi, vz] -> B6 over the whole half plane
-    launch_passA(planes_[P_PS], planes_[P_VZ]);
-    launch_passB<false>(gd_.nh);
-    launch_colfft<-1>(pb_, planes_[P_B5], gd_.nh);
-    launch_colfft<-1>(pb_ + S_, planes_[P_B6], gd_.nh);
+    launch_passA(planes_[P_PS], planes_[P_VZ], tf_, 1);
+    launch_passB<false>(gd_.nh, tf_, pb_, 1);
+    launch_colfft_mixed(pb_, planes_[P_B5]);
+    launch_colfft_mixed(pb_ + S_, planes_[P_B6]);
   }
   void shells(bool transfers, double* out5) override {
     if (transfers) brackets_full();
@@ -345,7 +351,9 @@ class EngineT final : public IEngine {
     cuda_check(cudaMemsetAsync(enc_, 0, sizeof(unsigned long long), st_), "memset");
     k_max_sq2<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_1], rplanes_[R_2], cnt, enc_);
     post("k_max_sq2");
-    k_cfl_dt<<<1, 1, 0, st_>>>(enc_, cfl_coef(cfl, mc), scal_, 0);
+    const CflCoef cc = cfl_coef(cfl, mc);
+    cuda_check(cudaMemcpyAsync(d_cfl_ + run_, &cc, sizeof(cc), cudaMemcpyHostToDevice, st_), "H2D cfl coef");
+    k_cfl_dt<<<1, 1, 0, st_>>>(enc_, d_cfl_ + run_, scal_, 0, 1);
     post("k_cfl_dt");
     return get_dt();
   }
@@ -355,7 +363,45 @@ class EngineT final : public IEngine {
   void set_time(double t) override { set_scal(1, t); }
   double get_dt() override { return get_scal(0); }
   double get_time() override { return get_scal(1); }
-  void mark_state_untruncated() override { dirty_ = true; }
+  void mark_state_untruncated() override { dirty_[run_] = 1; }
+  int nruns() const override { return nb_; }
+  void select_run(int r) override {
+    if (r < 0 || r >= nb_) throw Error(kEINVAL, "run index out of range");
+    run_ = r;
+    for (int p = 0; p < P_COUNT; ++p)
+      if (pbase_[p] && batched(p)) planes_[p] = pbase_[p] + (size_t)r * S_;
+    scal_ = scal_base_ + (size_t)r * kScalStride;
+    enc_ = enc_base_ + (size_t)r * kScalStride;
+  }
+  void set_run_coefs(const std::vector<ModelCoef>& mc) override {
+    if ((int)mc.size() != nb_) throw Error(kEINVAL, "one coefficient set per run");
+    coefs_ = mc;
+  }
+  void set_dt_all(double dt) override {
+    std::vector<double> h((size_t)kScalStride * nb_);
+    cuda_check(cudaMemcpyAsync(h.data(), scal_base_, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st_),
+               "D2H scal");
+    sync();
+    for (int r = 0; r < nb_; ++r) h[(size_t)r * kScalStride] = dt;
+    cuda_check(cudaMemcpyAsync(scal_base_, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st_),
+               "H2D scal");
+    sync();
+  }
+  void prepare_steps(double cfl) override {
+    truncate_if_dirty();
+    upload_coefs(coefs_.empty() ? ModelCoef{} : coefs_[0], cfl);
+  }
+  void enqueue_steps(bool cfl_mode) override { enqueue_step(cfl_mode, true, 0, nullptr); }
+  void get_scalars(double* dt, double* time) override {
+    std::vector<double> h((size_t)kScalStride * nb_);
+    cuda_check(cudaMemcpyAsync(h.data(), scal_base_, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st_),
+               "D2H scal");
+    sync();
+    for (int r = 0; r < nb_; ++r) {
+      if (dt) dt[r] = h[(size_t)r * kScalStride];
+      if (time) time[r] = h[(size_t)r * kScalStride + 1];
+    }
+  }
 
   void rand_force(const RandForceHost f[2]) override {
     RandForceArgs a = make_rf_args(f);
@@ -366,7 +412,8 @@ class EngineT final : public IEngine {
   void step(const ModelCoef& mc, bool cfl_mode, double cfl, bool add_time,
             const RandForceHost* rf) override {
     truncate_if_dirty();
-    enqueue_step(mc, cfl_mode, cfl, add_time, rf ? 1 : 0, rf);
+    upload_coefs(mc, cfl);
+    enqueue_step(cfl_mode, add_time, rf ? 1 : 0, rf);
   }
 
   void advance(const ModelCoef& mc, int nsteps, bool cfl_mode, double cfl,
@@ -389,7 +436,8 @@ class EngineT final : public IEngine {
       cuda_check(cudaMemsetAsync(d_ctr_, 0, sizeof(int), st_), "memset ctr");
       sync();  // seq goes out of scope
     }
-    GraphKey key{cfl_mode, rf != nullptr, cfl, mc};
+    upload_coefs(mc, cfl);
+    GraphKey key{cfl_mode, rf != nullptr};
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
@@ -397,7 +445,7 @@ class EngineT final : public IEngine {
       const int before = launches_;
       cuda_check(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal), "BeginCapture");
       try {
-        enqueue_step(mc, cfl_mode, cfl, true, rf ? -1 : 0, nullptr);
+        enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr);
       } catch (...) {
         cudaStreamEndCapture(st_, &g);
         if (g) cudaGraphDestroy(g);
@@ -455,7 +503,8 @@ class EngineT final : public IEngine {
     prof_.clear();
     profiling_ = true;
     try {
-      for (int s = 0; s < nsteps; ++s) enqueue_step(mc, false, 0.0, false, 0, nullptr);
+      upload_coefs(mc, 0.0);
+      for (int s = 0; s < nsteps; ++s) enqueue_step(false, false, 0, nullptr);
     } catch (...) {
       profiling_ = false;
       for (auto& e : prof_) {
@@ -482,15 +531,30 @@ class EngineT final : public IEngine {
   static constexpr int kSumBlocks = 304;  // 2 CTAs per SM on 152 SMs
   static constexpr double kPi = 3.1415926535897932384;
 
+  // The captured step depends only on these; coefficients and dt live in
+  // device arrays read by the kernels, so changing them needs no recapture.
   struct GraphKey {
     bool cfl_mode = false, rf = false;
-    double cfl = 0.0;
-    ModelCoef mc{};
-    bool same(const GraphKey& o) const {
-      return cfl_mode == o.cfl_mode && rf == o.rf && cfl == o.cfl &&
-             std::memcmp(&mc, &o.mc, sizeof(ModelCoef)) == 0;
-    }
+    bool same(const GraphKey& o) const { return cfl_mode == o.cfl_mode && rf == o.rf; }
   };
+  static bool batched(int p) { return p <= P_C2; }  // ps, vz, fp, fz, c1, c2
+  // per-run coefficient arrays: nb == 1 takes mc, a batch its run coefficients
+  void upload_coefs(const ModelCoef& mc, double cfl) {
+    if (nb_ == 1) coefs_.assign(1, mc);
+    if ((int)coefs_.size() != nb_) throw Error(kESTATE, "run coefficients not set");
+    std::vector<StepCoef> sc(nb_);
+    std::vector<CflCoef> cc(nb_);
+    for (int r = 0; r < nb_; ++r) {
+      const ModelCoef& m = coefs_[r];
+      sc[r] = StepCoef{m.nu, m.hnu, m.nuv, m.hnuv, 2 * m.omega, m.nn, m.mm, m.nnv, m.mmv};
+      cc[r] = cfl_coef(cfl, m);
+    }
+    cuda_check(cudaMemcpyAsync(d_sc_, sc.data(), sizeof(StepCoef) * nb_, cudaMemcpyHostToDevice, st_),
+               "H2D step coefs");
+    cuda_check(cudaMemcpyAsync(d_cfl_, cc.data(), sizeof(CflCoef) * nb_, cudaMemcpyHostToDevice, st_),
+               "H2D cfl coefs");
+    sync();
+  }
 
   template <typename U>
   U* alloc(size_t count) {
@@ -584,10 +648,15 @@ class EngineT final : public IEngine {
     return hsmall_[0];
   }
   void truncate_if_dirty() {
-    if (!dirty_) return;
-    specop(P_PS, P_PS, OP_TRUNC_RECT, 0.0);
-    specop(P_VZ, P_VZ, OP_TRUNC_RECT, 0.0);
-    dirty_ = false;
+    const int keep = run_;
+    for (int r = 0; r < nb_; ++r) {
+      if (!dirty_[r]) continue;
+      select_run(r);
+      specop(P_PS, P_PS, OP_TRUNC_RECT, 0.0);
+      specop(P_VZ, P_VZ, OP_TRUNC_RECT, 0.0);
+      dirty_[r] = 0;
+    }
+    select_run(keep);
   }
   RandForceArgs make_rf_args(const RandForceHost* f) {
     RandForceArgs a;
@@ -612,14 +681,16 @@ class EngineT final : public IEngine {
     return a;
   }
 
-  // rf_mode: 0 none, 1 single args (rf), -1 sequence from the device array
-  void enqueue_step(const ModelCoef& mc, bool cfl_mode, double cfl, bool add_time, int rf_mode,
-                    const RandForceHost* rf) {
-    StepCoef sc{mc.nu, mc.hnu, mc.nuv, mc.hnuv, 2 * mc.omega, mc.nn, mc.mm, mc.nnv, mc.mmv};
-    cpx<T>* ps = planes_[P_PS];
-    cpx<T>* vz = planes_[P_VZ];
-    cpx<T>* c1 = planes_[P_C1];
-    cpx<T>* c2 = planes_[P_C2];
+  // rf_mode: 0 none, 1 single args (rf), -1 sequence from the device array.
+  // All nb_ runs advance together (blockIdx.y = run); forcing draws and
+  // const_inj are single-run features.
+  void enqueue_step(bool cfl_mode, bool add_time, int rf_mode, const RandForceHost* rf) {
+    if (nb_ > 1 && (rf_mode != 0 || ci_on_)) throw Error(kEINVAL, "batched runs take constant forcing");
+    cpx<T>* ps = pbase_[P_PS];
+    cpx<T>* vz = pbase_[P_VZ];
+    cpx<T>* c1 = pbase_[P_C1];
+    cpx<T>* c2 = pbase_[P_C2];
+    const unsigned rb = (unsigned)((nb_ + 31) / 32);
     for (int o = 4; o >= 1; --o) {
       const cpx<T>* in1 = o == 4 ? ps : c1;
       const cpx<T>* in2 = o == 4 ? vz : c2;
@@ -629,28 +700,29 @@ class EngineT final : public IEngine {
         enqueue_const_inj(in1, o == 4 ? P_PS : P_C1, P_FP, 1, ci_fp0_);
         enqueue_const_inj(in2, o == 4 ? P_VZ : P_C2, P_FZ, 0, ci_fz0_);
       }
-      timed(0, [&] { launch_passA(in1, in2); });
+      timed(0, [&] { launch_passA(in1, in2, tf_, nb_); });
       if (o == 4 && cfl_mode) {
-        cuda_check(cudaMemsetAsync(enc_, 0, sizeof(unsigned long long), st_), "memset cfl");
-        launch_passB<true>(gd_.M);
-        k_cfl_dt<<<1, 1, 0, st_>>>(enc_, cfl_coef(cfl, mc), scal_, add_time ? 1 : 0);
+        cuda_check(cudaMemsetAsync(enc_base_, 0, sizeof(unsigned long long) * kScalStride * nb_, st_),
+                   "memset cfl");
+        launch_passB<true>(gd_.M, tf_, pb_, nb_);
+        k_cfl_dt<<<rb, 32, 0, st_>>>(enc_base_, d_cfl_, scal_base_, add_time ? 1 : 0, nb_);
         post("k_cfl_dt");
       } else {
-        timed(1, [&] { launch_passB<false>(gd_.M); });
+        timed(1, [&] { launch_passB<false>(gd_.M, tf_, pb_, nb_); });
         if (o == 4 && add_time) {
-          k_add_time<<<1, 1, 0, st_>>>(scal_);
+          k_add_time<<<rb, 32, 0, st_>>>(scal_base_, nb_);
           post("k_add_time");
         }
       }
       if (o == 4 && rf_mode == 1) {
         RandForceArgs a = make_rf_args(rf);
-        k_randforce<T><<<1, 1, 0, st_>>>(planes_[P_FP], planes_[P_FZ], scal_, a);
+        k_randforce<T><<<1, 1, 0, st_>>>(pbase_[P_FP], pbase_[P_FZ], scal_base_, a);
         post("k_randforce");
       } else if (o == 4 && rf_mode == -1) {
-        k_randforce_seq<T><<<1, 1, 0, st_>>>(planes_[P_FP], planes_[P_FZ], scal_, d_rf_, d_ctr_);
+        k_randforce_seq<T><<<1, 1, 0, st_>>>(pbase_[P_FP], pbase_[P_FZ], scal_base_, d_rf_, d_ctr_);
         post("k_randforce_seq");
       }
-      timed(2, [&] { launch_passC(in1, in2, out1, out2, sc, o); });
+      timed(2, [&] { launch_passC(in1, in2, out1, out2, o, nb_); });
     }
   }
 
@@ -661,7 +733,19 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       using C = Cfg<T, N>;
       auto k = k_colfft<T, N, DIR>;
-      k<<<(ncols + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(in, out, ncols, tw_);
+      k<<<(ncols + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(in, out, ncols, tw_, 0);
+      post("k_colfft");
+    });
+  }
+  // forward y-FFT of the nh columns of a product plane in the passes' mixed
+  // layout (pair-tiled in the FP32 tiled mode)
+  void launch_colfft_mixed(const cpx<T>* in, cpx<T>* out) {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      constexpr int PY = PassNT<T, N>::value;
+      using C = Cfg<T, N>;
+      auto k = k_colfft<T, N, -1, PY>;
+      k<<<(gd_.nh + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(in, out, gd_.nh, tw_, gd_.nh);
       post("k_colfft");
     });
   }
@@ -683,36 +767,42 @@ class EngineT final : public IEngine {
       post("k_rowr2c");
     });
   }
-  void launch_passA(const cpx<T>* a, const cpx<T>* b) {
+  Batch batch() const { return Batch{S_, (size_t)6 * gd_.M * n_, 2 * S_}; }
+  void launch_passA(const cpx<T>* a, const cpx<T>* b, cpx<T>* tf, int nb) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
-      using C = Cfg<T, N, PassNT<T, N>::value>;
+      constexpr int NT = PassNT<T, N>::value;
+      using C = Cfg<T, N, NT>;
       auto k = k_passA<T, N>;
-      k<<<(gd_.M + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(a, b, tf_, gd_, tw_);
+      const int groups = (gd_.M + NT - 1) / NT;
+      const dim3 grid((groups + C::G - 1) / C::G, nb);
+      k<<<grid, C::THREADS, C::SMEM, st_>>>(a, b, tf, gd_, tw_, batch());
       post("k_passA");
     });
   }
   template <bool CFL>
-  void launch_passB(int kxo) {
+  void launch_passB(int kxo, const cpx<T>* tf, cpx<T>* pb, int nb) {
     const T inv4 = (T)(1.0 / ((double)n_ * n_ * n_ * n_));
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       constexpr int NR = PassNT<T, N>::value;
       using C = Cfg<T, N, NR>;
       auto k = k_passB<T, N, CFL>;
-      k<<<(N / NR + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(tf_, pb_, kxo, gd_, inv4, tw_, enc_);
+      const dim3 grid((N / NR + C::G - 1) / C::G, nb);
+      k<<<grid, C::THREADS, C::SMEM, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
       post("k_passB");
     });
   }
-  void launch_passC(const cpx<T>* c1in, const cpx<T>* c2in, cpx<T>* c1out, cpx<T>* c2out,
-                    const StepCoef& sc, int o) {
+  void launch_passC(const cpx<T>* c1in, const cpx<T>* c2in, cpx<T>* c1out, cpx<T>* c2out, int o, int nb) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
-      using C = Cfg<T, N, PassNT<T, N>::value>;
+      constexpr int NT = PassNT<T, N>::value;
+      using C = Cfg<T, N, NT>;
       auto k = k_passC<T, N>;
-      k<<<(gd_.M + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(
-          pb_, c1in, c2in, planes_[P_PS], planes_[P_VZ], planes_[P_FP], planes_[P_FZ], c1out, c2out, gd_, sc,
-          scal_, o, tw_);
+      const int groups = (gd_.M + NT - 1) / NT;
+      const dim3 grid((groups + C::G - 1) / C::G, nb);
+      k<<<grid, C::THREADS, C::SMEM, st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ], pbase_[P_FP],
+                                           pbase_[P_FZ], c1out, c2out, gd_, d_sc_, scal_base_, o, tw_, batch());
       post("k_passC");
     });
   }
@@ -725,6 +815,7 @@ class EngineT final : public IEngine {
       constexpr size_t sm = Cfg<T, N>::SMEM;
       set_smem_attr(k_colfft<T, N, -1>, sm);
       set_smem_attr(k_colfft<T, N, +1>, sm);
+      set_smem_attr(k_colfft<T, N, -1, PassNT<T, N>::value>, sm);
       set_smem_attr(k_rowc2r<T, N>, sm);
       set_smem_attr(k_rowr2c<T, N>, sm);
       constexpr size_t smp = Cfg<T, N, PassNT<T, N>::value>::SMEM;
@@ -736,44 +827,28 @@ class EngineT final : public IEngine {
   }
 
   void build_twiddles() {
-    const int n = n_;
-    std::vector<double> c(n), s(n);
-    const double twopi = 2.0 * kPi;
-    for (int k = 0; k <= n / 8; ++k) {
-      const double a = twopi * (double)k / (double)n;
-      c[k] = std::cos(a);
-      s[k] = std::sin(a);
-    }
-    for (int k = n / 8 + 1; k <= n / 4; ++k) {
-      c[k] = s[n / 4 - k];
-      s[k] = c[n / 4 - k];
-    }
-    for (int k = n / 4 + 1; k <= n / 2; ++k) {
-      c[k] = -c[n / 2 - k];
-      s[k] = s[n / 2 - k];
-    }
-    for (int k = n / 2 + 1; k < n; ++k) {
-      c[k] = c[n - k];
-      s[k] = -s[n - k];
-    }
-    std::vector<tw_t<T>> h(n);
-    for (int k = 0; k < n; ++k) fill_tw(h[k], c[k], -s[k]);
-    cuda_check(cudaMemcpyAsync(tw_, h.data(), sizeof(tw_t<T>) * n, cudaMemcpyHostToDevice, st_), "H2D twiddles");
+    std::vector<double> c(n_), s(n_);
+    host_unit_roots(n_, c.data(), s.data());
+    std::vector<tw_t<T>> h(n_);
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      static_assert(BlockFFT<T, N, Cfg<T, N>::E>::TW_ELEMS <= N, "twiddle table fits in n entries");
+      build_stage_twiddles<T, N, Cfg<T, N>::E>(h.data(), c.data(), s.data());
+    });
+    cuda_check(cudaMemcpyAsync(tw_, h.data(), sizeof(tw_t<T>) * n_, cudaMemcpyHostToDevice, st_), "H2D twiddles");
     sync();
-  }
-  static void fill_tw(double2& w, double re, double im) {
-    w.x = re;
-    w.y = im;
-  }
-  static void fill_tw(float4& w, double re, double im) {
-    w.x = (float)re;
-    w.y = (float)im;
-    w.z = (float)(re - (double)w.x);
-    w.w = (float)(im - (double)w.y);
   }
 
   int n_, dev_;
   bool full_;
+  int nb_ = 1, run_ = 0;
+  cpx<T>* pbase_[P_COUNT] = {};
+  double* scal_base_ = nullptr;
+  unsigned long long* enc_base_ = nullptr;
+  StepCoef* d_sc_ = nullptr;
+  CflCoef* d_cfl_ = nullptr;
+  std::vector<char> dirty_;
+  std::vector<ModelCoef> coefs_;
   cudaStream_t st_ = nullptr;
   bool ci_on_ = false;
   int ci_n_ = 0;
@@ -801,7 +876,6 @@ class EngineT final : public IEngine {
   int* d_ctr_ = nullptr;
   int prev_[2][4] = {};
   int prev_n_[2] = {0, 0};
-  bool dirty_ = false;
   int launches_ = 0;
   cudaGraphExec_t graph_ = nullptr;
   int graph_launches_ = 0;

@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 namespace r2d3c {
 
 template <typename T> struct V2;
@@ -158,6 +160,24 @@ struct BlockFFT {
 
   static __device__ __forceinline__ int pad(int i) { return i + (i >> PADSH); }
 
+  // Radix of stage s, sub-transform size NS before stage s, and the offset of
+  // stage s's block in the stage-major twiddle table.  Block s holds, for
+  // every jm < NS(s), the R(s)-1 twiddles exp(-2 pi i r jm / (NS R)),
+  // r = 1..R-1, contiguously, so a thread's twiddles of one stage are one
+  // contiguous run and a warp's loads coalesce.
+  static __host__ __device__ constexpr int radix(int s) { return s == NST - 1 ? LAST_R : E; }
+  static __host__ __device__ constexpr int ns_of(int s) {
+    int ns = 1;
+    for (int i = 0; i < s; ++i) ns *= radix(i);
+    return ns;
+  }
+  static __host__ __device__ constexpr int tw_off(int s) {
+    int off = 0;
+    for (int i = 1; i < s; ++i) off += ns_of(i) * (radix(i) - 1);
+    return off;
+  }
+  static constexpr int TW_ELEMS = tw_off(NST) > 0 ? tw_off(NST) : 1;
+
   template <int DIR, int S, int NS>
   static __device__ __forceinline__ void stage(cpx<T> (&v)[NT][E], int lane, cpx<T>* sm,
                                                const tw_t<T>* __restrict__ tw) {
@@ -168,21 +188,20 @@ struct BlockFFT {
     for (int m = 0; m < B; ++m) {
       const int j = lane + m * TPF;
       const int jm = j & (NS - 1);
-      tw_t<T> w[R];
       if constexpr (NS > 1) {
-        constexpr int STR = N / (NS * R);
+        const tw_t<T>* tb = tw + tw_off(S) + jm * (R - 1);
 #pragma unroll
-        for (int r = 1; r < R; ++r) w[r] = __ldg(&tw[r * jm * STR]);
+        for (int r = 1; r < R; ++r) {
+          const tw_t<T> w = __ldg(&tb[r - 1]);
+#pragma unroll
+          for (int t = 0; t < NT; ++t) v[t][m + r * B] = twmul<DIR>(v[t][m + r * B], w);
+        }
       }
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
         cpx<T> u[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) u[r] = v[t][m + r * B];
-        if constexpr (NS > 1) {
-#pragma unroll
-          for (int r = 1; r < R; ++r) u[r] = twmul<DIR>(u[r], w[r]);
-        }
         RegDFT<T, R, DIR>::run(u);
 #pragma unroll
         for (int r = 0; r < R; ++r) v[t][m + r * B] = u[r];
@@ -233,5 +252,54 @@ struct BlockFFT {
     return sm[t * SMEM_ELEMS + pad(k)];
   }
 };
+
+// Host: the N-th roots of unity c[k] + i s[k] = exp(2 pi i k/N) in FP64 from
+// libm on the first octant and exact symmetries elsewhere.
+inline void host_unit_roots(int n, double* c, double* s) {
+  const double twopi = 2.0 * 3.1415926535897932384;
+  for (int k = 0; k <= n / 8; ++k) {
+    const double a = twopi * (double)k / (double)n;
+    c[k] = std::cos(a);
+    s[k] = std::sin(a);
+  }
+  for (int k = n / 8 + 1; k <= n / 4; ++k) {
+    c[k] = s[n / 4 - k];
+    s[k] = c[n / 4 - k];
+  }
+  for (int k = n / 4 + 1; k <= n / 2; ++k) {
+    c[k] = -c[n / 2 - k];
+    s[k] = s[n / 2 - k];
+  }
+  for (int k = n / 2 + 1; k < n; ++k) {
+    c[k] = c[n - k];
+    s[k] = -s[n - k];
+  }
+}
+
+inline void fill_tw(double2& w, double re, double im) {
+  w.x = re;
+  w.y = im;
+}
+inline void fill_tw(float4& w, double re, double im) {
+  w.x = (float)re;
+  w.y = (float)im;
+  w.z = (float)(re - (double)w.x);
+  w.w = (float)(im - (double)w.y);
+}
+
+// Host: the stage-major twiddle table of BlockFFT<T, N, E> (forward roots;
+// the inverse uses their conjugates).
+template <typename T, int N, int E>
+void build_stage_twiddles(tw_t<T>* out, const double* c, const double* s) {
+  using F = BlockFFT<T, N, E, 1>;
+  for (int st = 1; st < F::NST; ++st) {
+    const int ns = F::ns_of(st), r = F::radix(st), stride = N / (ns * r);
+    for (int jm = 0; jm < ns; ++jm)
+      for (int q = 1; q < r; ++q) {
+        const int k = q * jm * stride;
+        fill_tw(out[F::tw_off(st) + jm * (r - 1) + (q - 1)], c[k], -s[k]);
+      }
+  }
+}
 
 }  // namespace r2d3c

@@ -39,6 +39,15 @@ struct StepCoef {
   int nn, mm, nnv, mmv;
 };
 
+// Element strides between the runs of a batched launch (blockIdx.y = run):
+// spectral planes, the six derivative planes, the two product planes.  A
+// single run uses gridDim.y = 1.  Per-run scalars (dt, time, CFL maximum)
+// sit 8 entries apart.
+struct Batch {
+  size_t spec, tf, pb;
+};
+constexpr int kScalStride = 8;
+
 // Launch shape of a kernel carrying NT transforms per thread group: E
 // elements per thread, TPF = N/E threads per transform group, G groups per CTA.
 template <typename T, int N, int NT = 1>
@@ -51,13 +60,28 @@ struct Cfg {
   static constexpr size_t SMEM = (size_t)G * FFT::SMEM_BYTES;
 };
 
-// Transforms carried at once by one group in passes A, B and C: two in the
-// FP32 path (shared twiddles and barriers, two rows per 16-byte load in pass
-// B); one in the FP64 path, whose FP64 arithmetic is the bound and whose
-// register budget is already full.
+// Transforms carried at once by one group in passes A, B and C.  Two in the
+// FP32 path up to n = 4096 ("tiled" mode): pass A and C transform two
+// adjacent kx columns, pass B two adjacent rows, and the mixed planes use the
+// pair-tiled layout below so that every access moves whole 32-byte sectors.
+// One in the FP64 path (its FP64 arithmetic is the bound and its register
+// budget is full) and at n = 8192: plain column layout T[kx][y].
 template <typename T, int N> struct PassNT {
   static constexpr int value = (sizeof(T) == 4 && N <= 4096) ? 2 : 1;
 };
+
+// Mixed-plane element (kx, y) of a plane holding MX columns.  Column layout
+// (PY = 1 transform per group): kx*N + y.  Pair-tiled layout (PY = 2): rows
+// y = 2p, 2p+1 of all MX columns form one contiguous tile, each column's two
+// rows adjacent: ((y/2)*MX + kx)*2 + y%2.  Both layouts hold N*MX elements.
+template <int N, int PY>
+__host__ __device__ __forceinline__ size_t mix_idx(int kx, int y, int MX) {
+  if constexpr (PY == 2) {
+    return ((size_t)(y >> 1) * MX + kx) * 2 + (y & 1);
+  } else {
+    return (size_t)kx * N + y;
+  }
+}
 
 // ky value of row index j (Rot2D3C.para.f90:220-223)
 __device__ __forceinline__ int ky_of(int j, int n) { return j < (n >> 1) ? j : j - n; }
@@ -96,9 +120,10 @@ __device__ __forceinline__ T powi(T x, int k) {
 // generic y-direction transform of `ncols` contiguous columns of length N
 // (fftp2D.f90:208 forward, :251 inverse), in place allowed
 // --------------------------------------------------------------------------
-template <typename T, int N, int DIR>
+template <typename T, int N, int DIR, int PY = 1>
 __global__ void __launch_bounds__(Cfg<T, N>::THREADS)
-k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* __restrict__ tw) {
+k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* __restrict__ tw,
+         int mx_in = 0) {
   using C = Cfg<T, N>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
@@ -106,10 +131,10 @@ k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* _
   cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
   const int col = blockIdx.x * C::G + g;
   const bool ok = col < ncols;
-  const cpx<T>* src = in + (size_t)(ok ? col : 0) * N;
   cpx<T> v[1][C::E];
 #pragma unroll
-  for (int q = 0; q < C::E; ++q) v[0][q] = ok ? src[lane + q * C::TPF] : czero<T>();
+  for (int q = 0; q < C::E; ++q)
+    v[0][q] = ok ? in[mix_idx<N, PY>(col, lane + q * C::TPF, mx_in)] : czero<T>();
   F::template run<DIR>(v, lane, sm, tw);
   if (ok) {
     cpx<T>* dst = out + (size_t)col * N;
@@ -221,65 +246,84 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
 }
 
 // --------------------------------------------------------------------------
-// pass A: masked derivatives + inverse y-FFT, 6 fields per kx column, NT
-// fields at a time
+// pass A: masked derivatives + inverse y-FFT, 6 fields per kx column.  In
+// tiled mode each group transforms two adjacent columns at once and writes
+// both as 16-byte column pairs of the pair-tiled plane.
 // --------------------------------------------------------------------------
 template <typename T, int N>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __restrict__ tf,
-        DevGrid gd, const tw_t<T>* __restrict__ tw) {
+        DevGrid gd, const tw_t<T>* __restrict__ tw, Batch bs) {
   constexpr int NT = PassNT<T, N>::value;
+  ps += blockIdx.y * bs.spec;
+  vz += blockIdx.y * bs.spec;
+  tf += blockIdx.y * bs.tf;
   using C = Cfg<T, N, NT>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
-  const int col = blockIdx.x * C::G + g;
-  const bool ok = col < gd.M;
+  const int kx0 = (blockIdx.x * C::G + g) * NT;
   const size_t plane = (size_t)gd.M * N;
-  cpx<T> a[C::E], b[C::E];
-  T kyv[C::E], k2v[C::E];
-  const T kxv = (T)col;
+  int kyi[C::E];
 #pragma unroll
-  for (int q = 0; q < C::E; ++q) {
-    const int j = lane + q * C::TPF;
-    const int ky = ky_of(j, N);
-    const int k2 = col * col + ky * ky;
-    const bool in = ok && (ky <= gd.L && -ky <= gd.L) && k2 <= gd.kmaxi;
-    a[q] = in ? ps[(size_t)col * N + j] : czero<T>();
-    b[q] = in ? vz[(size_t)col * N + j] : czero<T>();
-    kyv[q] = (T)ky;
-    k2v[q] = (T)k2;
-  }
-  cpx<T> v[NT][C::E];
+  for (int q = 0; q < C::E; ++q) kyi[q] = ky_of(lane + q * C::TPF, N);
+  cpx<T> s[NT][C::E], v[NT][C::E];
 #pragma unroll 1
-  for (int f0 = 0; f0 < 6; f0 += NT) {
+  for (int src = 0; src < 2; ++src) {  // psi for fields 0-3, vz for fields 4-5
+    const cpx<T>* sp = src == 0 ? ps : vz;
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
-      const int f = f0 + t;
+      const int col = kx0 + t;
 #pragma unroll
       for (int q = 0; q < C::E; ++q) {
-        // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
-        const T k = (f & 1) ? kyv[q] : kxv;
-        cpx<T> s;
-        if (f < 2) {
-          s = a[q];
-        } else if (f < 4) {
-          const T m = -k2v[q];  // laplak2: -ka2*a
-          s = mkc<T>(m * a[q].x, m * a[q].y);
-        } else {
-          s = b[q];
-        }
-        v[t][q] = mkc<T>(-k * s.y, k * s.x);
+        const int ky = kyi[q];
+        const bool in = col < gd.M && (ky <= gd.L && -ky <= gd.L) && col * col + ky * ky <= gd.kmaxi;
+        s[t][q] = in ? sp[(size_t)col * N + lane + q * C::TPF] : czero<T>();
       }
     }
-    F::template run<+1>(v, lane, sm, tw);
-    if (ok) {
+#pragma unroll 1
+    for (int f = src * 4; f < (src == 0 ? 4 : 6); ++f) {
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
-        cpx<T>* dst = tf + (size_t)(f0 + t) * plane + (size_t)col * N;
+        const int col = kx0 + t;
 #pragma unroll
-        for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[t][q];
+        for (int q = 0; q < C::E; ++q) {
+          // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
+          const T k = (f & 1) ? (T)kyi[q] : (T)col;
+          cpx<T> x = s[t][q];
+          if (f == 2 || f == 3) {
+            const T m = -(T)(col * col + kyi[q] * kyi[q]);  // laplak2: -ka2*a
+            x = mkc<T>(m * x.x, m * x.y);
+          }
+          v[t][q] = mkc<T>(-k * x.y, k * x.x);
+        }
+      }
+      F::template run<+1>(v, lane, sm, tw);
+      cpx<T>* dst = tf + (size_t)f * plane;
+      if constexpr (NT == 2) {
+        // lanes (2p, 2p+1) hold rows y = 2p, 2p+1 of columns kx0, kx0+1: swap
+        // one value so each lane writes one column's row pair (16 bytes)
+        const bool odd = lane & 1;
+        const int kx = kx0 + (odd ? 1 : 0);
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          const cpx<T> give = odd ? v[0][q] : v[1][q];
+          cpx<T> got;
+          got.x = __shfl_xor_sync(0xffffffffu, give.x, 1);
+          got.y = __shfl_xor_sync(0xffffffffu, give.y, 1);
+          const int y = (lane + q * C::TPF) & ~1;
+          if (kx < gd.M) {
+            const cpx<T> lo = odd ? got : v[0][q];
+            const cpx<T> hi = odd ? v[1][q] : got;
+            *reinterpret_cast<float4*>(dst + mix_idx<N, 2>(kx, y, gd.M)) = make_float4(lo.x, lo.y, hi.x, hi.y);
+          }
+        }
+      } else {
+        if (kx0 < gd.M) {
+#pragma unroll
+          for (int q = 0; q < C::E; ++q) dst[(size_t)kx0 * N + lane + q * C::TPF] = v[0][q];
+        }
       }
     }
   }
@@ -317,8 +361,9 @@ __device__ __forceinline__ void packed_pair(const cpx<T>* __restrict__ pa, const
   if (k < M || k > N - M) {
     const int kk = k < M ? k : N - k;
     cpx<T> a[NR], b[NR];
-    load_rows<T, NR>(pa, (size_t)kk * N + y0, a);
-    load_rows<T, NR>(pb, (size_t)kk * N + y0, b);
+    const size_t off = mix_idx<N, NR>(kk, y0, M);
+    load_rows<T, NR>(pa, off, a);
+    load_rows<T, NR>(pb, off, b);
 #pragma unroll
     for (int t = 0; t < NR; ++t) {
       if (k == 0) {
@@ -342,8 +387,11 @@ __device__ __forceinline__ void packed_pair(const cpx<T>* __restrict__ pa, const
 template <typename T, int N, bool CFL>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
-        const tw_t<T>* __restrict__ tw, unsigned long long* __restrict__ cfl_enc) {
+        const tw_t<T>* __restrict__ tw, unsigned long long* __restrict__ cfl_enc, Batch bs) {
   constexpr int NR = PassNT<T, N>::value;
+  tf += blockIdx.y * bs.tf;
+  pb += blockIdx.y * bs.pb;
+  cfl_enc += blockIdx.y * kScalStride;
   using C = Cfg<T, N, NR>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
@@ -425,8 +473,9 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
         o1[t] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
         o2[t] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
       }
-      store_rows<T, NR>(pb, (size_t)k * N + y0, o1);
-      store_rows<T, NR>(pb + oplane, (size_t)k * N + y0, o2);
+      const size_t off = mix_idx<N, NR>(k, y0, gd.nh);
+      store_rows<T, NR>(pb, off, o1);
+      store_rows<T, NR>(pb + oplane, off, o2);
     }
   }
 }
@@ -470,50 +519,88 @@ template <typename T, int N>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         const cpx<T>* ps, const cpx<T>* vz, const cpx<T>* __restrict__ fp,
-        const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out, DevGrid gd, StepCoef sc,
-        const double* __restrict__ dtp, int o, const tw_t<T>* __restrict__ tw) {
+        const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out, DevGrid gd,
+        const StepCoef* __restrict__ scs, const double* __restrict__ scal, int o,
+        const tw_t<T>* __restrict__ tw, Batch bs) {
   constexpr int NT = PassNT<T, N>::value;
+  const size_t rs = blockIdx.y * bs.spec;
+  pb += blockIdx.y * bs.pb;
+  c1in += rs;
+  c2in += rs;
+  ps += rs;
+  vz += rs;
+  fp += rs;
+  fz += rs;
+  c1out += rs;
+  c2out += rs;
+  const StepCoef sc = scs[blockIdx.y];
+  const double* dtp = scal + blockIdx.y * kScalStride;
   using C = Cfg<T, N, NT>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
-  const int col = blockIdx.x * C::G + g;
-  const bool ok = col < gd.M;
+  const int kx0 = (blockIdx.x * C::G + g) * NT;
   const size_t oplane = (size_t)gd.nh * N;
-  const cpx<T>* s5 = pb + (size_t)(ok ? col : 0) * N;
-  cpx<T> c56[2][C::E];
-#pragma unroll
-  for (int q = 0; q < C::E; ++q) {
-    c56[0][q] = s5[lane + q * C::TPF];
-    c56[1][q] = s5[oplane + lane + q * C::TPF];
-  }
+  cpx<T> c5[NT][C::E], c6[NT][C::E];
   if constexpr (NT == 2) {
-    F::template run<-1>(c56, lane, sm, tw);
+    // lane pair (2p, 2p+1): the even lane loads column kx0's rows (2p, 2p+1),
+    // the odd lane column kx0+1's; one swap gives each lane its own row of
+    // both columns
+    const bool odd = lane & 1;
+    const int kx = kx0 + (odd ? 1 : 0);
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      const int y = (lane + q * C::TPF) & ~1;
+      const size_t off = mix_idx<N, 2>(kx, y, gd.nh);
+#pragma unroll
+      for (int pl = 0; pl < 2; ++pl) {
+        const float4 w = __ldg(reinterpret_cast<const float4*>(pb + pl * oplane + off));
+        const float gx = odd ? w.x : w.z, gy = odd ? w.y : w.w;  // value the partner needs
+        const float rx = __shfl_xor_sync(0xffffffffu, gx, 1);
+        const float ry = __shfl_xor_sync(0xffffffffu, gy, 1);
+        cpx<T> mine0, mine1;  // (column kx0, my row), (column kx0+1, my row)
+        if (odd) {
+          mine0 = mkc<T>(rx, ry);
+          mine1 = mkc<T>(w.z, w.w);
+        } else {
+          mine0 = mkc<T>(w.x, w.y);
+          mine1 = mkc<T>(rx, ry);
+        }
+        if (pl == 0) {
+          c5[0][q] = mine0;
+          c5[1][q] = mine1;
+        } else {
+          c6[0][q] = mine0;
+          c6[1][q] = mine1;
+        }
+      }
+    }
+    F::template run<-1>(c5, lane, sm, tw);
+    F::template run<-1>(c6, lane, sm, tw);
   } else {
-    cpx<T> a[1][C::E], b[1][C::E];
+    const cpx<T>* s5 = pb + (size_t)(kx0 < gd.M ? kx0 : 0) * N;
 #pragma unroll
     for (int q = 0; q < C::E; ++q) {
-      a[0][q] = c56[0][q];
-      b[0][q] = c56[1][q];
+      c5[0][q] = s5[lane + q * C::TPF];
+      c6[0][q] = s5[oplane + lane + q * C::TPF];
     }
-    F::template run<-1>(a, lane, sm, tw);
-    F::template run<-1>(b, lane, sm, tw);
-#pragma unroll
-    for (int q = 0; q < C::E; ++q) {
-      c56[0][q] = a[0][q];
-      c56[1][q] = b[0][q];
-    }
+    F::template run<-1>(c5, lane, sm, tw);
+    F::template run<-1>(c6, lane, sm, tw);
   }
-  if (!ok) return;
   const T tmp1 = (T)(*dtp / (double)o);  // :581
 #pragma unroll
-  for (int q = 0; q < C::E; ++q) {
-    const int j = lane + q * C::TPF;
-    const int ky = ky_of(j, N);
-    if (ky > gd.L || -ky > gd.L) continue;
-    rk_update<T>(c56[0][q], c56[1][q], (size_t)col * N + j, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp, fz,
-                 c1out, c2out, sc, tmp1, gd.kmaxi);
+  for (int t = 0; t < NT; ++t) {
+    const int col = kx0 + t;
+    if (col >= gd.M) continue;
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      const int j = lane + q * C::TPF;
+      const int ky = ky_of(j, N);
+      if (ky > gd.L || -ky > gd.L) continue;
+      rk_update<T>(c5[t][q], c6[t][q], (size_t)col * N + j, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp,
+                   fz, c1out, c2out, sc, tmp1, gd.kmaxi);
+    }
   }
 }
 

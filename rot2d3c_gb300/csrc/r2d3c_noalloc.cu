@@ -63,29 +63,19 @@ int tw_offset(int n) {  // start of the n-point table inside g_noalloc_tw
   return off;
 }
 
-// Same construction as the engines' tables: octant symmetry around libm
-// values in FP64, tw[k] = exp(-2 pi i k / n).
+// The stage-major tables of the column and row kernels for one n, from the
+// same FP64 roots as the engines' tables.
 void host_twiddles(int n, double2* out) {
-  const double twopi = 2.0 * 3.1415926535897932384;
   std::vector<double> c(n), s(n);
-  for (int k = 0; k <= n / 8; ++k) {
-    const double a = twopi * (double)k / (double)n;
-    c[k] = std::cos(a);
-    s[k] = std::sin(a);
+  host_unit_roots(n, c.data(), s.data());
+  switch (n) {
+    case 16: build_stage_twiddles<double, 16, Cfg<double, 16>::E>(out, c.data(), s.data()); break;
+    case 32: build_stage_twiddles<double, 32, Cfg<double, 32>::E>(out, c.data(), s.data()); break;
+    case 64: build_stage_twiddles<double, 64, Cfg<double, 64>::E>(out, c.data(), s.data()); break;
+    case 128: build_stage_twiddles<double, 128, Cfg<double, 128>::E>(out, c.data(), s.data()); break;
+    case 256: build_stage_twiddles<double, 256, Cfg<double, 256>::E>(out, c.data(), s.data()); break;
+    default: build_stage_twiddles<double, 512, Cfg<double, 512>::E>(out, c.data(), s.data()); break;
   }
-  for (int k = n / 8 + 1; k <= n / 4; ++k) {
-    c[k] = s[n / 4 - k];
-    s[k] = c[n / 4 - k];
-  }
-  for (int k = n / 4 + 1; k <= n / 2; ++k) {
-    c[k] = -c[n / 2 - k];
-    s[k] = s[n / 2 - k];
-  }
-  for (int k = n / 2 + 1; k < n; ++k) {
-    c[k] = c[n - k];
-    s[k] = -s[n - k];
-  }
-  for (int k = 0; k < n; ++k) out[k] = make_double2(c[k], -s[k]);
 }
 
 // Per-device set-up, run by the first call on each device (with that device
