@@ -789,7 +789,7 @@ class EngineT final : public IEngine {
       using C = Cfg<T, N, NR>;
       auto k = k_passB<T, N, CFL>;
       const dim3 grid((N / NR + C::G - 1) / C::G, nb);
-      k<<<grid, C::THREADS, C::SMEM, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
+      k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
       post("k_passB");
     });
   }
@@ -801,7 +801,7 @@ class EngineT final : public IEngine {
       auto k = k_passC<T, N>;
       const int groups = (gd_.M + NT - 1) / NT;
       const dim3 grid((groups + C::G - 1) / C::G, nb);
-      k<<<grid, C::THREADS, C::SMEM, st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ], pbase_[P_FP],
+      k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ], pbase_[P_FP],
                                            pbase_[P_FZ], c1out, c2out, gd_, d_sc_, scal_base_, o, tw_, batch());
       post("k_passC");
     });
@@ -819,10 +819,11 @@ class EngineT final : public IEngine {
       set_smem_attr(k_rowc2r<T, N>, sm);
       set_smem_attr(k_rowr2c<T, N>, sm);
       constexpr size_t smp = Cfg<T, N, PassNT<T, N>::value>::SMEM;
+      constexpr size_t smh = PassSmem<T, N>::SMEM;
       set_smem_attr(k_passA<T, N>, smp);
-      set_smem_attr(k_passB<T, N, true>, smp);
-      set_smem_attr(k_passB<T, N, false>, smp);
-      set_smem_attr(k_passC<T, N>, smp);
+      set_smem_attr(k_passB<T, N, true>, smh);
+      set_smem_attr(k_passB<T, N, false>, smh);
+      set_smem_attr(k_passC<T, N>, smh);
     });
   }
 

@@ -161,10 +161,10 @@ struct BlockFFT {
   static __device__ __forceinline__ int pad(int i) { return i + (i >> PADSH); }
 
   // Radix of stage s, sub-transform size NS before stage s, and the offset of
-  // stage s's block in the stage-major twiddle table.  Block s holds, for
-  // every jm < NS(s), the R(s)-1 twiddles exp(-2 pi i r jm / (NS R)),
-  // r = 1..R-1, contiguously, so a thread's twiddles of one stage are one
-  // contiguous run and a warp's loads coalesce.
+  // stage s's block in the stage-major twiddle table.  Block s holds the
+  // twiddles exp(-2 pi i r jm / (NS R)), r = 1..R-1, jm < NS(s), r-major:
+  // entry (r-1)*NS + jm, so that the threads of a warp (consecutive jm) read
+  // one contiguous run for each r.
   static __host__ __device__ constexpr int radix(int s) { return s == NST - 1 ? LAST_R : E; }
   static __host__ __device__ constexpr int ns_of(int s) {
     int ns = 1;
@@ -189,10 +189,10 @@ struct BlockFFT {
       const int j = lane + m * TPF;
       const int jm = j & (NS - 1);
       if constexpr (NS > 1) {
-        const tw_t<T>* tb = tw + tw_off(S) + jm * (R - 1);
+        const tw_t<T>* tb = tw + tw_off(S) + jm;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          const tw_t<T> w = __ldg(&tb[r - 1]);
+          const tw_t<T> w = __ldg(&tb[(r - 1) * NS]);
 #pragma unroll
           for (int t = 0; t < NT; ++t) v[t][m + r * B] = twmul<DIR>(v[t][m + r * B], w);
         }
@@ -297,7 +297,7 @@ void build_stage_twiddles(tw_t<T>* out, const double* c, const double* s) {
     for (int jm = 0; jm < ns; ++jm)
       for (int q = 1; q < r; ++q) {
         const int k = q * jm * stride;
-        fill_tw(out[F::tw_off(st) + jm * (r - 1) + (q - 1)], c[k], -s[k]);
+        fill_tw(out[F::tw_off(st) + (q - 1) * ns + jm], c[k], -s[k]);
       }
   }
 }

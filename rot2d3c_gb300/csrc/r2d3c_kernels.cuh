@@ -70,6 +70,20 @@ template <typename T, int N> struct PassNT {
   static constexpr int value = (sizeof(T) == 4 && N <= 4096) ? 2 : 1;
 };
 
+// Shared memory of passes B and C: NT transform buffers per group, plus (when
+// it fits) a store for the first transform's result, which is held across the
+// later transforms (pass B: dx psi + i dy psi; pass C: the [psi,-k^2 psi]
+// column) -- keeping it out of registers avoids spills.
+template <typename T, int N>
+struct PassSmem {
+  static constexpr int NT = PassNT<T, N>::value;
+  using C = Cfg<T, N, NT>;
+  static constexpr size_t HOLD_BYTES = (size_t)NT * N * sizeof(cpx<T>);
+  static constexpr bool HOLD = C::FFT::SMEM_BYTES + HOLD_BYTES <= 200 * 1024;
+  static constexpr size_t GROUP_ELEMS = (size_t)NT * C::FFT::SMEM_ELEMS + (HOLD ? (size_t)NT * N : 0);
+  static constexpr size_t SMEM = (size_t)C::G * GROUP_ELEMS * sizeof(cpx<T>);
+};
+
 // Mixed-plane element (kx, y) of a plane holding MX columns.  Column layout
 // (PY = 1 transform per group): kx*N + y.  Pair-tiled layout (PY = 2): rows
 // y = 2p, 2p+1 of all MX columns form one contiguous tile, each column's two
@@ -389,6 +403,8 @@ __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
         const tw_t<T>* __restrict__ tw, unsigned long long* __restrict__ cfl_enc, Batch bs) {
   constexpr int NR = PassNT<T, N>::value;
+  using PS = PassSmem<T, N>;
+  constexpr bool HOLD = PS::HOLD;
   tf += blockIdx.y * bs.tf;
   pb += blockIdx.y * bs.pb;
   cfl_enc += blockIdx.y * kScalStride;
@@ -396,14 +412,16 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  cpx<T>* sm = smbase_ + (size_t)g * NR * F::SMEM_ELEMS;
+  cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
+  cpx<T>* hold = sm + NR * F::SMEM_ELEMS;  // z1 store (HOLD)
   int rg = blockIdx.x * C::G + g;
   const bool ok = rg < N / NR;
   if (!ok) rg = 0;  // surplus groups recompute rows 0.. and store nothing
   const int y0 = rg * NR;
   const int M = gd.M;
   const size_t plane = (size_t)M * N;
-  cpx<T> z1[NR][C::E], v[NR][C::E];
+  cpx<T> v[NR][C::E];
+  cpx<T> z1r[HOLD ? 1 : NR][C::E];
   T p1[NR][C::E];
   // pair (d_x psi, d_y psi)
 #pragma unroll
@@ -411,22 +429,34 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
     cpx<T> z[NR];
     packed_pair<T, N, NR>(tf, tf + plane, lane + q * C::TPF, y0, M, z);
 #pragma unroll
-    for (int t = 0; t < NR; ++t) z1[t][q] = z[t];
+    for (int t = 0; t < NR; ++t) v[t][q] = z[t];
   }
-  F::template run<+1>(z1, lane, sm, tw);
+  F::template run<+1>(v, lane, sm, tw);
   if constexpr (CFL) {
     double m = 0.0;
 #pragma unroll
     for (int t = 0; t < NR; ++t)
 #pragma unroll
       for (int q = 0; q < C::E; ++q) {
-        const double rx = (double)z1[t][q].x, ry = (double)z1[t][q].y;
+        const double rx = (double)v[t][q].x, ry = (double)v[t][q].y;
         m = fmax(m, rx * rx + ry * ry);
       }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(cfl_enc, enc_ordered(m));
   }
+  // each thread reads back only the positions it wrote: no barrier needed
+  auto z1 = [&](int t, int q) -> cpx<T> {
+    if constexpr (HOLD) return hold[t * N + lane + q * C::TPF];
+    else return z1r[t][q];
+  };
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      if constexpr (HOLD) hold[t * N + lane + q * C::TPF] = v[t][q];
+      else z1r[t][q] = v[t][q];
+    }
   // pair (d_x(-k^2 psi), d_y(-k^2 psi)) -> [psi, -k^2 psi]
 #pragma unroll
   for (int q = 0; q < C::E; ++q) {
@@ -439,8 +469,10 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
 #pragma unroll
   for (int t = 0; t < NR; ++t)
 #pragma unroll
-    for (int q = 0; q < C::E; ++q)
-      p1[t][q] = (z1[t][q].x * v[t][q].y - z1[t][q].y * v[t][q].x) * inv_n4;
+    for (int q = 0; q < C::E; ++q) {
+      const cpx<T> a = z1(t, q);
+      p1[t][q] = (a.x * v[t][q].y - a.y * v[t][q].x) * inv_n4;
+    }
   // pair (d_x vz, d_y vz) -> [psi, vz]
 #pragma unroll
   for (int q = 0; q < C::E; ++q) {
@@ -453,8 +485,10 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
 #pragma unroll
   for (int t = 0; t < NR; ++t)
 #pragma unroll
-    for (int q = 0; q < C::E; ++q)
-      v[t][q] = mkc<T>(p1[t][q], (z1[t][q].x * v[t][q].y - z1[t][q].y * v[t][q].x) * inv_n4);
+    for (int q = 0; q < C::E; ++q) {
+      const cpx<T> a = z1(t, q);
+      v[t][q] = mkc<T>(p1[t][q], (a.x * v[t][q].y - a.y * v[t][q].x) * inv_n4);
+    }
   // forward x-FFT of both real products at once
   F::template run<-1>(v, lane, sm, tw);
   F::to_smem(v, lane, sm);
@@ -523,6 +557,8 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         const StepCoef* __restrict__ scs, const double* __restrict__ scal, int o,
         const tw_t<T>* __restrict__ tw, Batch bs) {
   constexpr int NT = PassNT<T, N>::value;
+  using PS = PassSmem<T, N>;
+  constexpr bool HOLD = PS::HOLD;
   const size_t rs = blockIdx.y * bs.spec;
   pb += blockIdx.y * bs.pb;
   c1in += rs;
@@ -539,55 +575,54 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
-  cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
+  cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
+  cpx<T>* hold = sm + NT * F::SMEM_ELEMS;  // transformed [psi,-k^2 psi] columns (HOLD)
   const int kx0 = (blockIdx.x * C::G + g) * NT;
   const size_t oplane = (size_t)gd.nh * N;
-  cpx<T> c5[NT][C::E], c6[NT][C::E];
-  if constexpr (NT == 2) {
-    // lane pair (2p, 2p+1): the even lane loads column kx0's rows (2p, 2p+1),
-    // the odd lane column kx0+1's; one swap gives each lane its own row of
-    // both columns
-    const bool odd = lane & 1;
-    const int kx = kx0 + (odd ? 1 : 0);
+  cpx<T> v[NT][C::E];
+  cpx<T> c5r[HOLD ? 1 : NT][C::E];
+#pragma unroll 1
+  for (int pl = 0; pl < 2; ++pl) {
+    const cpx<T>* src = pb + pl * oplane;
+    if constexpr (NT == 2) {
+      // lane pair (2p, 2p+1): the even lane loads column kx0's rows (2p, 2p+1),
+      // the odd lane column kx0+1's; one swap gives each lane its own row of
+      // both columns
+      const bool odd = lane & 1;
+      const int kx = kx0 + (odd ? 1 : 0);
 #pragma unroll
-    for (int q = 0; q < C::E; ++q) {
-      const int y = (lane + q * C::TPF) & ~1;
-      const size_t off = mix_idx<N, 2>(kx, y, gd.nh);
-#pragma unroll
-      for (int pl = 0; pl < 2; ++pl) {
-        const float4 w = __ldg(reinterpret_cast<const float4*>(pb + pl * oplane + off));
+      for (int q = 0; q < C::E; ++q) {
+        const int y = (lane + q * C::TPF) & ~1;
+        const float4 w = __ldg(reinterpret_cast<const float4*>(src + mix_idx<N, 2>(kx, y, gd.nh)));
         const float gx = odd ? w.x : w.z, gy = odd ? w.y : w.w;  // value the partner needs
         const float rx = __shfl_xor_sync(0xffffffffu, gx, 1);
         const float ry = __shfl_xor_sync(0xffffffffu, gy, 1);
-        cpx<T> mine0, mine1;  // (column kx0, my row), (column kx0+1, my row)
         if (odd) {
-          mine0 = mkc<T>(rx, ry);
-          mine1 = mkc<T>(w.z, w.w);
+          v[0][q] = mkc<T>(rx, ry);
+          v[1][q] = mkc<T>(w.z, w.w);
         } else {
-          mine0 = mkc<T>(w.x, w.y);
-          mine1 = mkc<T>(rx, ry);
-        }
-        if (pl == 0) {
-          c5[0][q] = mine0;
-          c5[1][q] = mine1;
-        } else {
-          c6[0][q] = mine0;
-          c6[1][q] = mine1;
+          v[0][q] = mkc<T>(w.x, w.y);
+          v[1][q] = mkc<T>(rx, ry);
         }
       }
-    }
-    F::template run<-1>(c5, lane, sm, tw);
-    F::template run<-1>(c6, lane, sm, tw);
-  } else {
-    const cpx<T>* s5 = pb + (size_t)(kx0 < gd.M ? kx0 : 0) * N;
+    } else {
+      const cpx<T>* s5 = src + (size_t)(kx0 < gd.M ? kx0 : 0) * N;
 #pragma unroll
-    for (int q = 0; q < C::E; ++q) {
-      c5[0][q] = s5[lane + q * C::TPF];
-      c6[0][q] = s5[oplane + lane + q * C::TPF];
+      for (int q = 0; q < C::E; ++q) v[0][q] = s5[lane + q * C::TPF];
     }
-    F::template run<-1>(c5, lane, sm, tw);
-    F::template run<-1>(c6, lane, sm, tw);
+    F::template run<-1>(v, lane, sm, tw);
+    if (pl == 0) {
+#pragma unroll
+      for (int t = 0; t < NT; ++t)
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          if constexpr (HOLD) hold[t * N + lane + q * C::TPF] = v[t][q];
+          else c5r[t][q] = v[t][q];
+        }
+    }
   }
+  // v holds the transformed [psi, vz] columns; c5 is read back per element
+  // by the thread that stored it (no barrier needed)
   const T tmp1 = (T)(*dtp / (double)o);  // :581
 #pragma unroll
   for (int t = 0; t < NT; ++t) {
@@ -598,7 +633,10 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
       const int j = lane + q * C::TPF;
       const int ky = ky_of(j, N);
       if (ky > gd.L || -ky > gd.L) continue;
-      rk_update<T>(c5[t][q], c6[t][q], (size_t)col * N + j, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp,
+      cpx<T> c5;
+      if constexpr (HOLD) c5 = hold[t * N + j];
+      else c5 = c5r[t][q];
+      rk_update<T>(c5, v[t][q], (size_t)col * N + j, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp,
                    fz, c1out, c2out, sc, tmp1, gd.kmaxi);
     }
   }
