@@ -96,6 +96,7 @@ class EngineT final : public IEngine {
       }
       tg_ = alloc<cpx<T>>(S_);
       tw_ = alloc<tw_t<T>>((size_t)n);
+      tw_a_ = alloc<tw_t<T>>((size_t)n);  // pass A's stage schedule
       stage_count_ = std::max(2 * S_, (size_t)n * n);
       if (!std::is_same<T, double>::value) stage64_ = alloc<double>(stage_count_);
       scal_base_ = scal_ = alloc<double>((size_t)kScalStride * nb_);
@@ -772,11 +773,11 @@ class EngineT final : public IEngine {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       constexpr int NT = PassNT<T, N>::value;
-      using C = Cfg<T, N, NT>;
+      using C = CfgA<T, N>;
       auto k = k_passA<T, N>;
       const int groups = (gd_.M + NT - 1) / NT;
       const dim3 grid((groups + C::G - 1) / C::G, nb);
-      k<<<grid, C::THREADS, C::SMEM, st_>>>(a, b, tf, gd_, tw_, batch());
+      k<<<grid, C::THREADS, C::SMEM, st_>>>(a, b, tf, gd_, tw_a_, batch());
       post("k_passA");
     });
   }
@@ -818,9 +819,8 @@ class EngineT final : public IEngine {
       set_smem_attr(k_colfft<T, N, -1, PassNT<T, N>::value>, sm);
       set_smem_attr(k_rowc2r<T, N>, sm);
       set_smem_attr(k_rowr2c<T, N>, sm);
-      constexpr size_t smp = Cfg<T, N, PassNT<T, N>::value>::SMEM;
       constexpr size_t smh = PassSmem<T, N>::SMEM;
-      set_smem_attr(k_passA<T, N>, smp);
+      set_smem_attr(k_passA<T, N>, CfgA<T, N>::SMEM);
       set_smem_attr(k_passB<T, N, true>, smh);
       set_smem_attr(k_passB<T, N, false>, smh);
       set_smem_attr(k_passC<T, N>, smh);
@@ -830,13 +830,18 @@ class EngineT final : public IEngine {
   void build_twiddles() {
     std::vector<double> c(n_), s(n_);
     host_unit_roots(n_, c.data(), s.data());
-    std::vector<tw_t<T>> h(n_);
+    std::vector<tw_t<T>> h(n_), ha(n_);
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
+      constexpr int EA = PassAE<T, N>::value;
       static_assert(BlockFFT<T, N, Cfg<T, N>::E>::TW_ELEMS <= N, "twiddle table fits in n entries");
+      static_assert(BlockFFT<T, N, EA>::TW_ELEMS <= N, "twiddle table fits in n entries");
       build_stage_twiddles<T, N, Cfg<T, N>::E>(h.data(), c.data(), s.data());
+      build_stage_twiddles<T, N, EA>(ha.data(), c.data(), s.data());
     });
     cuda_check(cudaMemcpyAsync(tw_, h.data(), sizeof(tw_t<T>) * n_, cudaMemcpyHostToDevice, st_), "H2D twiddles");
+    cuda_check(cudaMemcpyAsync(tw_a_, ha.data(), sizeof(tw_t<T>) * n_, cudaMemcpyHostToDevice, st_),
+               "H2D twiddles");
     sync();
   }
 
@@ -866,6 +871,7 @@ class EngineT final : public IEngine {
   cpx<T>* pb_ = nullptr;
   cpx<T>* tg_ = nullptr;
   tw_t<T>* tw_ = nullptr;
+  tw_t<T>* tw_a_ = nullptr;
   double* stage64_ = nullptr;
   double* scal_ = nullptr;
   unsigned long long* enc_ = nullptr;

@@ -50,9 +50,9 @@ constexpr int kScalStride = 8;
 
 // Launch shape of a kernel carrying NT transforms per thread group: E
 // elements per thread, TPF = N/E threads per transform group, G groups per CTA.
-template <typename T, int N, int NT = 1>
+template <typename T, int N, int NT = 1, int EOVR = 0>
 struct Cfg {
-  static constexpr int E = (N >= 8192) ? 16 : 8;
+  static constexpr int E = EOVR ? EOVR : (N >= 8192 ? 16 : 8);
   using FFT = BlockFFT<T, N, E, NT>;
   static constexpr int TPF = N / E;
   static constexpr int G = TPF >= 256 ? 1 : 256 / TPF;  // transform groups per CTA
@@ -69,6 +69,16 @@ struct Cfg {
 template <typename T, int N> struct PassNT {
   static constexpr int value = (sizeof(T) == 4 && N <= 4096) ? 2 : 1;
 };
+
+// Elements per thread of pass A: radix-16 (256 threads, room for 255
+// registers, two exchanges per transform) for the FP32 4096 grid, where it
+// measured faster; the default radix elsewhere.  Pass A then needs the
+// twiddle table of its own stage schedule.
+template <typename T, int N> struct PassAE {
+  static constexpr int value = (sizeof(T) == 4 && N == 4096) ? 16 : Cfg<T, N>::E;
+};
+template <typename T, int N>
+using CfgA = Cfg<T, N, PassNT<T, N>::value, PassAE<T, N>::value>;
 
 // Shared memory of passes B and C: NT transform buffers per group, plus (when
 // it fits) a store for the first transform's result, which is held across the
@@ -265,14 +275,14 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
 // both as 16-byte column pairs of the pair-tiled plane.
 // --------------------------------------------------------------------------
 template <typename T, int N>
-__global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
+__global__ void __launch_bounds__(CfgA<T, N>::THREADS, 1)
 k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __restrict__ tf,
         DevGrid gd, const tw_t<T>* __restrict__ tw, Batch bs) {
   constexpr int NT = PassNT<T, N>::value;
   ps += blockIdx.y * bs.spec;
   vz += blockIdx.y * bs.spec;
   tf += blockIdx.y * bs.tf;
-  using C = Cfg<T, N, NT>;
+  using C = CfgA<T, N>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
