@@ -463,9 +463,17 @@ def main():
               for i, k in enumerate("ABC")}
     top = max("ABC", key=lambda k: passes[k]["ms_per_launch"])
     ach = passes[top]["achieved_gbs"]
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"pass_traffic_fp32_n{n}.json")
+    if os.path.exists(tpath):  # DRAM bytes per launch from the committed ncu capture
+        with open(tpath) as f:
+            tr = json.load(f).get(f"k_pass{top}")
+        if tr:
+            traffic = tr["dram_read"] + tr["dram_write"]
     roofline = {"bound": "hbm", "kernel": f"k_pass{top} (FP32, n={n})", "achieved": ach, "peak": hbm,
                 "unit": "GB/s", "frac": ach / hbm, "peak_source": peak_kind,
-                "traffic": None, "passes": passes,
+                "traffic": traffic, "traffic_source": "profiles/pass_traffic_fp32_n4096.json (ncu)",
+                "algorithmic_bytes_per_launch": pass_bytes(n, 4)[top], "passes": passes,
                 "step_share": {k: ms32[i] * cnt32[i] / sum(ms32[j] * cnt32[j] for j in range(4))
                                for i, k in enumerate("ABC")}}
 

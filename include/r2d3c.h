@@ -198,6 +198,28 @@ int r2d3c_ensemble_cond_check(r2d3c_ensemble* ens, int run, double time, double 
 int r2d3c_ensemble_spectrum(r2d3c_ensemble* ens, int run, double* Ek, double* Ezk);
 int r2d3c_ensemble_kernel_launches(const r2d3c_ensemble* ens, long long* count);
 
+/* ---- Learned subgrid closure (no counterpart in the reference) --------- */
+/* A periodic CNN of six 3x3 convolutions, 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2
+   channels with GELU between layers, BF16 operands and FP32 accumulation on
+   the tensor cores, FP32 master parameters trained with Adam.  Tensors are
+   device FP32 NHWC arrays on an H x W periodic grid (H % 8 == 0,
+   W % 16 == 0): inputs [batch][H][W][8], outputs/targets [batch][H][W][2].
+   The parameter vector is layer by layer: weights [9][cin][cout] (tap =
+   3*dy + dx, input pixel (y+dy-1, x+dx-1)) then biases [cout]. */
+typedef struct r2d3c_cnn r2d3c_cnn;
+int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** cnn);
+int r2d3c_cnn_destroy(r2d3c_cnn* cnn);
+int r2d3c_cnn_num_params(const r2d3c_cnn* cnn, long long* n);
+int r2d3c_cnn_get_params(r2d3c_cnn* cnn, float* host);
+int r2d3c_cnn_set_params(r2d3c_cnn* cnn, const float* host);
+int r2d3c_cnn_forward(r2d3c_cnn* cnn, const float* d_x, int batch, float* d_out);
+/* loss = mean squared error over all outputs; host_grad (may be NULL)
+   receives dloss/dparams */
+int r2d3c_cnn_gradients(r2d3c_cnn* cnn, const float* d_x, const float* d_y, int batch, float* host_grad,
+                        double* loss);
+/* forward, backward and one Adam step (beta 0.9/0.999, eps 1e-8) */
+int r2d3c_cnn_train_step(r2d3c_cnn* cnn, const float* d_x, const float* d_y, int batch, float lr, double* loss);
+
 /* ---- Level 2 operators (reference subroutines on host arrays) ---------- */
 /* derivk2 (pseudospec2D_Rot2D3C.f90:6-68) */
 int r2d3c_derivk2(r2d3c_ctx* ctx, const double* a, double* b, int dir);

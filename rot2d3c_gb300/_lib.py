@@ -101,6 +101,14 @@ SIGNATURES = {
     "r2d3c_ensemble_cond_check": (C.c_int, [_P, C.c_int, C.c_double, _D]),
     "r2d3c_ensemble_spectrum": (C.c_int, [_P, C.c_int, _D, _D]),
     "r2d3c_ensemble_kernel_launches": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "r2d3c_cnn_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_P)]),
+    "r2d3c_cnn_destroy": (C.c_int, [_P]),
+    "r2d3c_cnn_num_params": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "r2d3c_cnn_get_params": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "r2d3c_cnn_set_params": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "r2d3c_cnn_forward": (C.c_int, [_P, _P, C.c_int, _P]),
+    "r2d3c_cnn_gradients": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(C.c_float), _D]),
+    "r2d3c_cnn_train_step": (C.c_int, [_P, _P, _P, C.c_int, C.c_float, _D]),
     "r2d3c_derivk2": (C.c_int, [_P, _D, _D, C.c_int]),
     "r2d3c_laplak2": (C.c_int, [_P, _D, _D]),
     "r2d3c_inv_laplak2": (C.c_int, [_P, _D, _D]),

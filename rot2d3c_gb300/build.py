@@ -17,7 +17,9 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librot2d3c_gb300.so")
-SOURCES = ["r2d3c_api.cu", "r2d3c_engine_f64.cu", "r2d3c_engine_f32.cu", "r2d3c_noalloc.cu"]
+SOURCES = [
+    "r2d3c_api.cu", "r2d3c_engine_f64.cu", "r2d3c_engine_f32.cu", "r2d3c_noalloc.cu", "r2d3c_cnn.cu",
+]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 

@@ -1,0 +1,65 @@
+"""Learned subgrid closure over the C-ABI (r2d3c_cnn_*): the CNN and its
+training, on device tensors (torch CUDA tensors or raw device pointers)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import check, load
+
+CIN = [8, 32, 32, 32, 32, 32]
+COUT = [32, 32, 32, 32, 32, 2]
+
+
+def _ptr(t) -> C.c_void_p:
+    return C.c_void_p(t if isinstance(t, int) else t.data_ptr())
+
+
+class CNN:
+    """The closure network on an H x W periodic grid (see include/r2d3c.h)."""
+
+    def __init__(self, H: int, W: int, max_batch: int, seed: int = 0):
+        self.H, self.W, self.max_batch = H, W, max_batch
+        h = C.c_void_p()
+        check(load().r2d3c_cnn_create(H, W, max_batch, seed, C.byref(h)), "cnn_create")
+        self._h = h
+        n = C.c_longlong()
+        check(load().r2d3c_cnn_num_params(self._h, C.byref(n)), "cnn_num_params")
+        self.nparams = n.value
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.nparams, np.float32)
+        check(load().r2d3c_cnn_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float))), "cnn_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.nparams
+        check(load().r2d3c_cnn_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))), "cnn_set_params")
+
+    def forward(self, x, batch: int, out) -> None:
+        check(load().r2d3c_cnn_forward(self._h, _ptr(x), batch, _ptr(out)), "cnn_forward")
+
+    def gradients(self, x, y, batch: int):
+        g = np.empty(self.nparams, np.float32)
+        loss = C.c_double()
+        check(load().r2d3c_cnn_gradients(self._h, _ptr(x), _ptr(y), batch, g.ctypes.data_as(C.POINTER(C.c_float)),
+                                         C.byref(loss)), "cnn_gradients")
+        return loss.value, g
+
+    def train_step(self, x, y, batch: int, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        check(load().r2d3c_cnn_train_step(self._h, _ptr(x), _ptr(y), batch, lr, C.byref(loss)), "cnn_train_step")
+        return loss.value
+
+    def destroy(self) -> None:
+        if getattr(self, "_h", None):
+            load().r2d3c_cnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

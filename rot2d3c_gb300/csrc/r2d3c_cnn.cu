@@ -1,0 +1,619 @@
+// Learned subgrid closure: a small periodic CNN (6 layers of 3x3 convolution,
+// 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2 channels, GELU between layers) with
+// BF16 operands and FP32 accumulation on the tensor cores, trained with Adam
+// by the kernels of this file.  No counterpart in the reference.
+//
+// Activations are NHWC (channels fastest) on an H x W periodic grid, batch B.
+// Every convolution is an implicit GEMM: out[p][co] = sum_{tap, ci}
+// in[p + offset(tap)][ci] * w[tap*CIN + ci][co], tap = (dy, dx) in 3x3,
+// computed by warp-level mma.sync m16n8k16 (bf16 x bf16 -> f32) from a
+// shared-memory halo tile of the input and the weights.  Backward data is the
+// same convolution of dY with the tap-flipped, channel-transposed weights;
+// backward weights is the GEMM dW[k][co] = sum_p in_col[p][k] dY[p][co],
+// split over persistent CTAs with a fixed-order reduction of the partials.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/r2d3c.h"
+#include "r2d3c_engine.h"
+
+namespace r2d3c {
+std::string& last_error_slot();
+}
+
+namespace {
+
+using namespace r2d3c;
+using bf16 = __nv_bfloat16;
+
+constexpr int kLayers = 6;
+constexpr int kCinPad[kLayers] = {16, 32, 32, 32, 32, 32};   // input channels (layer 0 padded 8 -> 16)
+constexpr int kCoutPad[kLayers] = {32, 32, 32, 32, 32, 16};  // output channels (last padded 2 -> 16)
+constexpr int kCin[kLayers] = {8, 32, 32, 32, 32, 32};
+constexpr int kCout[kLayers] = {32, 32, 32, 32, 32, 2};
+
+// tile of the implicit GEMM: 8 rows x 16 columns of pixels, 8 warps, one
+// 16-pixel row per warp
+constexpr int TH = 8, TW = 16, kThreads = 256;
+
+__device__ __forceinline__ unsigned pack_bf16(bf16 lo, bf16 hi) {
+  return (unsigned)__bfloat16_as_ushort(lo) | ((unsigned)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+// ---------------------------------------------------------------------------
+// out[p][co] = sum_k in_col[p][k] w[k][co] (+ bias), periodic 3x3 stencil.
+// in: [B][H][W][CIN] bf16; w: [9*CIN][COUT] bf16; y: [B][H][W][COUT] f32
+// (pre-activation, may be null); a: [B][H][W][COUT] bf16 = act(y) (may be
+// null); act: 0 identity, 1 GELU.  Requires H % TH == 0, W % TW == 0.
+// ---------------------------------------------------------------------------
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kThreads)
+k_conv(const bf16* __restrict__ in, const bf16* __restrict__ w, const float* __restrict__ bias, int H, int W,
+       float* __restrict__ y, bf16* __restrict__ a, int act, int cout_store) {
+  constexpr int NTN = COUT / 8;  // n-tiles
+  __shared__ __align__(16) bf16 s_in[(TH + 2) * (TW + 2) * CIN];
+  __shared__ __align__(16) bf16 s_w[9 * CIN * COUT];
+  const int tiles_x = W / TW, tiles_y = H / TH;
+  const int t = blockIdx.x;
+  const int b = t / (tiles_x * tiles_y);
+  const int ty0 = ((t / tiles_x) % tiles_y) * TH, tx0 = (t % tiles_x) * TW;
+  // stage the weights and the halo tile (periodic wrap)
+  for (int i = threadIdx.x; i < 9 * CIN * COUT / 8; i += kThreads)
+    reinterpret_cast<uint4*>(s_w)[i] = reinterpret_cast<const uint4*>(w)[i];
+  constexpr int VPP = CIN / 8;  // 16-byte vectors per pixel
+  for (int i = threadIdx.x; i < (TH + 2) * (TW + 2) * VPP; i += kThreads) {
+    const int v = i % VPP, px = (i / VPP) % (TW + 2), py = (i / VPP) / (TW + 2);
+    const int gy = (ty0 + py - 1 + H) % H, gx = (tx0 + px - 1 + W) % W;
+    reinterpret_cast<uint4*>(s_in)[i] =
+        reinterpret_cast<const uint4*>(in + (((size_t)b * H + gy) * W + gx) * CIN)[v];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  float acc[NTN][4];
+#pragma unroll
+  for (int n = 0; n < NTN; ++n)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[n][r] = 0.f;
+  // warp handles tile row `warp`, pixels x = 0..15 of the tile
+#pragma unroll
+  for (int tap = 0; tap < 9; ++tap) {
+    const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+    for (int c0 = 0; c0 < CIN; c0 += 16) {
+      // A (16 x 16): rows = pixels gid and gid+8, cols = channels c0 + tig*2 (+1, +8, +9)
+      const bf16* r0 = s_in + ((warp + dy) * (TW + 2) + (gid + dx)) * CIN + c0 + tig * 2;
+      const bf16* r1 = s_in + ((warp + dy) * (TW + 2) + (gid + 8 + dx)) * CIN + c0 + tig * 2;
+      unsigned af[4];
+      af[0] = *reinterpret_cast<const unsigned*>(r0);
+      af[1] = *reinterpret_cast<const unsigned*>(r1);
+      af[2] = *reinterpret_cast<const unsigned*>(r0 + 8);
+      af[3] = *reinterpret_cast<const unsigned*>(r1 + 8);
+      const int k0 = tap * CIN + c0;
+#pragma unroll
+      for (int n = 0; n < NTN; ++n) {
+        // B (16 x 8): rows k = k0 + tig*2 (+1, +8, +9), col co = n*8 + gid
+        const int co = n * 8 + gid;
+        unsigned bfr[2];
+        bfr[0] = pack_bf16(s_w[(k0 + tig * 2) * COUT + co], s_w[(k0 + tig * 2 + 1) * COUT + co]);
+        bfr[1] = pack_bf16(s_w[(k0 + tig * 2 + 8) * COUT + co], s_w[(k0 + tig * 2 + 9) * COUT + co]);
+        mma_bf16(acc[n], af, bfr);
+      }
+    }
+  }
+  // D: rows gid, gid+8 (pixels), cols n*8 + tig*2 (+1)
+  const int gy = ty0 + warp;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const int gx = tx0 + gid + half * 8;
+    const size_t pix = ((size_t)b * H + gy) * W + gx;
+#pragma unroll
+    for (int n = 0; n < NTN; ++n)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int co = n * 8 + tig * 2 + e;
+        if (co >= cout_store) continue;
+        float v = acc[n][half * 2 + e] + (bias ? bias[co] : 0.f);
+        if (y) y[pix * cout_store + co] = v;
+        if (a) a[pix * COUT + co] = __float2bfloat16_rn(act ? gelu(v) : v);
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dW[k][co] partials: CTA c accumulates over pixel tiles c, c + grid, ...
+// in: [B][H][W][CIN] bf16, dy: [B][H][W][COUT] bf16; part: [grid][9*CIN*COUT]
+// ---------------------------------------------------------------------------
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kThreads)
+k_conv_wgrad(const bf16* __restrict__ in, const bf16* __restrict__ dy, int H, int W, int ntiles,
+             float* __restrict__ part) {
+  constexpr int K = 9 * CIN, MT = K / 16, NTN = COUT / 8, PAIRS = MT * NTN;
+  constexpr int PPW = (PAIRS + 7) / 8;  // (m,n) tile pairs per warp
+  __shared__ __align__(16) bf16 s_in[(TH + 2) * (TW + 2) * CIN];
+  __shared__ __align__(16) bf16 s_dy[TH * TW * COUT];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  float acc[PPW][4];
+#pragma unroll
+  for (int i = 0; i < PPW; ++i)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[i][r] = 0.f;
+  const int tiles_x = W / TW, tiles_y = H / TH;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int b = t / (tiles_x * tiles_y);
+    const int ty0 = ((t / tiles_x) % tiles_y) * TH, tx0 = (t % tiles_x) * TW;
+    __syncthreads();
+    constexpr int VPP = CIN / 8;
+    for (int i = threadIdx.x; i < (TH + 2) * (TW + 2) * VPP; i += kThreads) {
+      const int v = i % VPP, px = (i / VPP) % (TW + 2), py = (i / VPP) / (TW + 2);
+      const int gy = (ty0 + py - 1 + H) % H, gx = (tx0 + px - 1 + W) % W;
+      reinterpret_cast<uint4*>(s_in)[i] =
+          reinterpret_cast<const uint4*>(in + (((size_t)b * H + gy) * W + gx) * CIN)[v];
+    }
+    constexpr int VPO = COUT / 8;
+    for (int i = threadIdx.x; i < TH * TW * VPO; i += kThreads) {
+      const int v = i % VPO, px = (i / VPO) % TW, py = (i / VPO) / TW;
+      reinterpret_cast<uint4*>(s_dy)[i] =
+          reinterpret_cast<const uint4*>(dy + (((size_t)b * H + ty0 + py) * W + tx0 + px) * COUT)[v];
+    }
+    __syncthreads();
+    // reduction over the 128 pixels of the tile in 8 k-steps of 16 (one tile row each)
+#pragma unroll 1
+    for (int ks = 0; ks < TH; ++ks) {
+#pragma unroll
+      for (int i = 0; i < PPW; ++i) {
+        const int pair = warp * PPW + i;
+        if (pair >= PAIRS) break;
+        const int mt = pair / NTN, nt = pair % NTN;
+        // A (16 x 16) = in_col^T: rows m = k index mt*16 + gid (+8), cols = pixels tig*2 (+1, +8, +9)
+        unsigned af[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {      // rows gid, gid + 8
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {    // pixel columns tig*2 + c*8
+            const int k = mt * 16 + gid + h * 8;
+            const int tap = k / CIN, ci = k % CIN, dyy = tap / 3, dxx = tap % 3;
+            const int px = tig * 2 + c * 8;
+            const bf16 v0 = s_in[((ks + dyy) * (TW + 2) + px + dxx) * CIN + ci];
+            const bf16 v1 = s_in[((ks + dyy) * (TW + 2) + px + 1 + dxx) * CIN + ci];
+            af[h + 2 * c] = pack_bf16(v0, v1);
+          }
+        }
+        // B (16 x 8) = dY: rows = pixels tig*2 (+1, +8, +9), col = co nt*8 + gid
+        const int co = nt * 8 + gid;
+        unsigned bfr[2];
+        bfr[0] = pack_bf16(s_dy[(ks * TW + tig * 2) * COUT + co], s_dy[(ks * TW + tig * 2 + 1) * COUT + co]);
+        bfr[1] = pack_bf16(s_dy[(ks * TW + tig * 2 + 8) * COUT + co], s_dy[(ks * TW + tig * 2 + 9) * COUT + co]);
+        mma_bf16(acc[i], af, bfr);
+      }
+    }
+  }
+  float* out = part + (size_t)blockIdx.x * K * COUT;
+#pragma unroll
+  for (int i = 0; i < PPW; ++i) {
+    const int pair = warp * PPW + i;
+    if (pair >= PAIRS) break;
+    const int mt = pair / NTN, nt = pair % NTN;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+        out[(size_t)(mt * 16 + gid + h * 8) * COUT + nt * 8 + tig * 2 + e] = acc[i][h * 2 + e];
+  }
+}
+
+// grad[i] = sum_c part[c][i] in fixed order; optional bias gradient from dy
+__global__ void k_reduce_parts(const float* __restrict__ part, int nparts, int count, float* __restrict__ grad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float s = 0.f;
+  for (int c = 0; c < nparts; ++c) s += part[(size_t)c * count + i];
+  grad[i] = s;
+}
+
+// db[co] = sum_p dy[p][co] (one CTA per channel, fixed-order tree)
+__global__ void k_bias_grad(const bf16* __restrict__ dy, size_t npix, int cstride, float* __restrict__ db) {
+  const int co = blockIdx.x;
+  __shared__ float red[256];
+  float s = 0.f;
+  for (size_t p = threadIdx.x; p < npix; p += blockDim.x) s += __bfloat162float(dy[p * cstride + co]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[co] = red[0];
+}
+
+// dY' = dA * gelu'(y) (bf16), for the hidden layers
+__global__ void k_gelu_back(const bf16* __restrict__ da, const float* __restrict__ y, size_t count,
+                            bf16* __restrict__ dy) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    dy[i] = __float2bfloat16_rn(__bfloat162float(da[i]) * gelu_d(y[i]));
+}
+
+// MSE loss of the 2 output channels against the target; dY of the last
+// layer (padded to 16 channels, zero beyond 2) and per-CTA loss partials
+__global__ void k_mse(const float* __restrict__ out, const float* __restrict__ tgt, size_t npix, float scale,
+                      bf16* __restrict__ dy, float* __restrict__ lpart) {
+  __shared__ float red[256];
+  float s = 0.f;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npix; p += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      float g = 0.f;
+      if (c < 2) {
+        const float d = out[p * 2 + c] - tgt[p * 2 + c];
+        s += d * d;
+        g = 2.f * d * scale;
+      }
+      dy[p * 16 + c] = __float2bfloat16_rn(g);
+    }
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) lpart[blockIdx.x] = red[0];
+}
+
+// Adam on FP32 master weights; also writes the bf16 forward weights
+// wf[k][co] (padded shapes) and the backward-data weights wb[k'][ci] with
+// k' = (8 - tap)*COUTP + co.
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, int count, float lr, float b1, float b2, float eps, float bc1,
+                       float bc2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+// master weights [9][cin][cout] (unpadded) -> wf [9*CINP][COUTP], wb [9*COUTP][CINP]
+__global__ void k_pack_weights(const float* __restrict__ wm, int cin, int cout, int cinp, int coutp,
+                               bf16* __restrict__ wf, bf16* __restrict__ wb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 9 * cinp * coutp) return;
+  const int co = i % coutp, ci = (i / coutp) % cinp, tap = i / (coutp * cinp);
+  const float v = (ci < cin && co < cout) ? wm[((size_t)tap * cin + ci) * cout + co] : 0.f;
+  wf[((size_t)tap * cinp + ci) * coutp + co] = __float2bfloat16_rn(v);
+  wb[((size_t)(8 - tap) * coutp + co) * cinp + ci] = __float2bfloat16_rn(v);
+}
+
+// padded weight gradient [9][cinp][coutp] -> parameter layout [9][cin][cout]
+__global__ void k_unpad_wgrad(const float* __restrict__ gp, int cin, int cout, int cinp, int coutp,
+                              float* __restrict__ g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 9 * cin * cout) return;
+  const int co = i % cout, ci = (i / cout) % cin, tap = i / (cout * cin);
+  g[i] = gp[((size_t)tap * cinp + ci) * coutp + co];
+}
+
+// FP32 NHWC [npix][c] -> bf16 NHWC [npix][cp] (zero padding channels)
+__global__ void k_to_bf16(const float* __restrict__ x, size_t npix, int c, int cp, bf16* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix * cp; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t p = i / cp;
+    const int ch = (int)(i % cp);
+    out[i] = __float2bfloat16_rn(ch < c ? x[p * c + ch] : 0.f);
+  }
+}
+
+// unpadded dX of layer 0's input is not needed; bias-gradient buffers etc.
+struct Layer {
+  int cin, cout, cinp, coutp;
+  size_t woff, boff;  // offsets in the parameter vector
+};
+
+template <int CIN, int COUT>
+void conv_launch(const bf16* in, const bf16* w, const float* b, int B, int H, int W, float* y, bf16* a, int act,
+                 int cout_store, cudaStream_t st) {
+  const int tiles = B * (H / TH) * (W / TW);
+  k_conv<CIN, COUT><<<tiles, kThreads, 0, st>>>(in, w, b, H, W, y, a, act, cout_store);
+}
+
+template <int CIN, int COUT>
+void wgrad_launch(const bf16* in, const bf16* dy, int B, int H, int W, float* part, int nparts, cudaStream_t st) {
+  const int tiles = B * (H / TH) * (W / TW);
+  k_conv_wgrad<CIN, COUT><<<nparts, kThreads, 0, st>>>(in, dy, H, W, tiles, part);
+}
+
+}  // namespace
+
+struct r2d3c_cnn {
+  int H = 0, W = 0, Bmax = 0;
+  cudaStream_t st = nullptr;
+  Layer L[kLayers];
+  size_t nparam = 0;
+  float *wm = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;  // master params, grads, Adam moments
+  bf16* wf[kLayers] = {};
+  bf16* wb[kLayers] = {};
+  bf16* act[kLayers + 1] = {};   // act[0] = bf16 input (16 ch), act[l+1] = layer l output (bf16)
+  float* pre[kLayers] = {};      // pre-activations y (f32), last = network output (2 ch)
+  bf16 *dA = nullptr, *dY = nullptr;
+  float* part = nullptr;
+  float* lpart = nullptr;
+  int nparts = 304;
+  long long step = 0;
+  std::vector<void*> owned;
+  template <typename U>
+  U* alloc(size_t n) {
+    void* p = nullptr;
+    cuda_check(cudaMalloc(&p, n * sizeof(U)), "cudaMalloc (cnn)");
+    owned.push_back(p);
+    return static_cast<U*>(p);
+  }
+  ~r2d3c_cnn() {
+    for (void* p : owned) cudaFree(p);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  void conv(int l, const bf16* in, const bf16* w, int B, float* y, bf16* a, int act_on, bool bias, bool back) {
+    const float* b = bias ? wm + L[l].boff : nullptr;
+    // forward shapes (CINP, COUTP) or backward-data shapes (COUTP, CINP)
+    const int ci = back ? L[l].coutp : L[l].cinp, co = back ? L[l].cinp : L[l].coutp;
+    const int store = back ? co : (l == kLayers - 1 ? L[l].cout : co);
+    if (ci == 16 && co == 32) conv_launch<16, 32>(in, w, b, B, H, W, y, a, act_on, store, st);
+    else if (ci == 32 && co == 32) conv_launch<32, 32>(in, w, b, B, H, W, y, a, act_on, store, st);
+    else if (ci == 32 && co == 16) conv_launch<32, 16>(in, w, b, B, H, W, y, a, act_on, store, st);
+    else throw Error(kEINVAL, "unsupported conv shape");
+    cuda_check(cudaGetLastError(), "k_conv");
+  }
+  void wgrad(int l, const bf16* in, const bf16* dy, int B) {
+    const int ci = L[l].cinp, co = L[l].coutp;
+    if (ci == 16 && co == 32) wgrad_launch<16, 32>(in, dy, B, H, W, part, nparts, st);
+    else if (ci == 32 && co == 32) wgrad_launch<32, 32>(in, dy, B, H, W, part, nparts, st);
+    else if (ci == 32 && co == 16) wgrad_launch<32, 16>(in, dy, B, H, W, part, nparts, st);
+    else throw Error(kEINVAL, "unsupported wgrad shape");
+    cuda_check(cudaGetLastError(), "k_conv_wgrad");
+  }
+
+  // forward of a batch of B inputs (f32 NHWC 8 ch) -> pre[kLayers-1] (f32 NHWC 2 ch)
+  void forward(const float* x, int B) {
+    const size_t npix = (size_t)B * H * W;
+    k_to_bf16<<<1024, 256, 0, st>>>(x, npix, 8, 16, act[0]);
+    cuda_check(cudaGetLastError(), "k_to_bf16");
+    for (int l = 0; l < kLayers; ++l) {
+      const bool last = l == kLayers - 1;
+      conv(l, act[l], wf[l], B, pre[l], last ? nullptr : act[l + 1], last ? 0 : 1, true, false);
+    }
+  }
+
+  // gradients of the MSE loss into grad[]; returns the loss (host sync)
+  double backward(const float* tgt, int B) {
+    const size_t npix = (size_t)B * H * W;
+    const float scale = 1.0f / (float)(npix * 2);
+    k_mse<<<256, 256, 0, st>>>(pre[kLayers - 1], tgt, npix, scale, dY, lpart);
+    cuda_check(cudaGetLastError(), "k_mse");
+    for (int l = kLayers - 1; l >= 0; --l) {
+      const Layer& ly = L[l];
+      // dY holds dL/dy of layer l (bf16, coutp channels)
+      wgrad(l, act[l], dY, B);
+      const int kc = 9 * ly.cinp * ly.coutp;
+      k_reduce_parts<<<(kc + 255) / 256, 256, 0, st>>>(part, nparts, kc, part + (size_t)nparts * kc);
+      cuda_check(cudaGetLastError(), "k_reduce_parts");
+      // unpad into grad (layout [9][cin][cout])
+      unpad_wgrad(l, part + (size_t)nparts * kc);
+      k_bias_grad<<<ly.cout, 256, 0, st>>>(dY, npix, ly.coutp, grad + ly.boff);
+      cuda_check(cudaGetLastError(), "k_bias_grad");
+      if (l == 0) break;
+      // dA of layer l-1 = conv(dY, wb[l]); then dY' = dA * gelu'(pre[l-1])
+      conv(l, dY, wb[l], B, nullptr, dA, 0, false, true);
+      k_gelu_back<<<1024, 256, 0, st>>>(dA, pre[l - 1], npix * L[l - 1].coutp, dY);
+      cuda_check(cudaGetLastError(), "k_gelu_back");
+    }
+    std::vector<float> lp(256);
+    cuda_check(cudaMemcpyAsync(lp.data(), lpart, 256 * sizeof(float), cudaMemcpyDeviceToHost, st), "D2H loss");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    double s = 0.0;
+    for (float v : lp) s += v;
+    return s / (double)(npix * 2);
+  }
+
+  void unpad_wgrad(int l, const float* gp) {
+    const Layer& ly = L[l];
+    const int c = 9 * ly.cin * ly.cout;
+    k_unpad_wgrad<<<(c + 255) / 256, 256, 0, st>>>(gp, ly.cin, ly.cout, ly.cinp, ly.coutp, grad + ly.woff);
+    cuda_check(cudaGetLastError(), "k_unpad_wgrad");
+  }
+
+  void pack() {
+    for (int l = 0; l < kLayers; ++l) {
+      const Layer& ly = L[l];
+      const int c = 9 * ly.cinp * ly.coutp;
+      k_pack_weights<<<(c + 255) / 256, 256, 0, st>>>(wm + ly.woff, ly.cin, ly.cout, ly.cinp, ly.coutp, wf[l], wb[l]);
+      cuda_check(cudaGetLastError(), "k_pack_weights");
+    }
+  }
+
+  void adam(float lr) {
+    ++step;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float bc1 = 1.f - std::pow(b1, (float)step), bc2 = 1.f - std::pow(b2, (float)step);
+    k_adam<<<(int)((nparam + 255) / 256), 256, 0, st>>>(wm, grad, am, av, (int)nparam, lr, b1, b2, eps, bc1, bc2);
+    cuda_check(cudaGetLastError(), "k_adam");
+    pack();
+  }
+};
+
+namespace {
+int fail(const Error& e) {
+  last_error_slot() = e.what();
+  return e.code;
+}
+}  // namespace
+
+extern "C" {
+
+int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** out) {
+  try {
+    if (!out) throw Error(kEINVAL, "NULL argument");
+    *out = nullptr;
+    if (H < TH || W < TW || H % TH || W % TW) throw Error(kEINVAL, "H must be a multiple of 8 and W of 16");
+    if (max_batch < 1) throw Error(kEINVAL, "max_batch must be >= 1");
+    std::unique_ptr<r2d3c_cnn> c(new r2d3c_cnn());
+    c->H = H;
+    c->W = W;
+    c->Bmax = max_batch;
+    cuda_check(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate");
+    size_t off = 0;
+    for (int l = 0; l < kLayers; ++l) {
+      c->L[l] = Layer{kCin[l], kCout[l], kCinPad[l], kCoutPad[l], off, 0};
+      off += (size_t)9 * kCin[l] * kCout[l];
+      c->L[l].boff = off;
+      off += kCout[l];
+    }
+    c->nparam = off;
+    c->wm = c->alloc<float>(off);
+    c->grad = c->alloc<float>(off);
+    c->am = c->alloc<float>(off);
+    c->av = c->alloc<float>(off);
+    cuda_check(cudaMemsetAsync(c->am, 0, off * sizeof(float), c->st), "memset");
+    cuda_check(cudaMemsetAsync(c->av, 0, off * sizeof(float), c->st), "memset");
+    cuda_check(cudaMemsetAsync(c->grad, 0, off * sizeof(float), c->st), "memset");
+    // Kaiming-uniform weights (fan_in = 9 cin), zero biases, seeded
+    std::vector<float> h(off, 0.f);
+    std::mt19937 rng((unsigned)seed);
+    for (int l = 0; l < kLayers; ++l) {
+      const float bound = std::sqrt(6.0f / (9.0f * (float)kCin[l])) * (l == kLayers - 1 ? 0.1f : 1.0f);
+      std::uniform_real_distribution<float> U(-bound, bound);
+      for (size_t i = 0; i < (size_t)9 * kCin[l] * kCout[l]; ++i) h[c->L[l].woff + i] = U(rng);
+    }
+    cuda_check(cudaMemcpyAsync(c->wm, h.data(), off * sizeof(float), cudaMemcpyHostToDevice, c->st), "H2D");
+    const size_t npix = (size_t)max_batch * H * W;
+    for (int l = 0; l < kLayers; ++l) {
+      c->wf[l] = c->alloc<bf16>((size_t)9 * kCinPad[l] * kCoutPad[l]);
+      c->wb[l] = c->alloc<bf16>((size_t)9 * kCinPad[l] * kCoutPad[l]);
+      c->pre[l] = c->alloc<float>(npix * (l == kLayers - 1 ? kCout[l] : kCoutPad[l]));
+    }
+    c->act[0] = c->alloc<bf16>(npix * 16);
+    for (int l = 0; l < kLayers; ++l) c->act[l + 1] = c->alloc<bf16>(npix * kCoutPad[l]);
+    c->dA = c->alloc<bf16>(npix * 32);
+    c->dY = c->alloc<bf16>(npix * 32);  // dL/dy of the current layer (<= 32 channels)
+    c->part = c->alloc<float>((size_t)(c->nparts + 1) * 9 * 32 * 32);
+    c->lpart = c->alloc<float>(256);
+    c->pack();
+    cuda_check(cudaStreamSynchronize(c->st), "sync");
+    *out = c.release();
+  } catch (const Error& e) {
+    return fail(e);
+  } catch (const std::exception& e) {
+    last_error_slot() = e.what();
+    return R2D3C_EINVAL;
+  }
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_destroy(r2d3c_cnn* c) {
+  delete c;
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_num_params(const r2d3c_cnn* c, long long* n) {
+  if (!c || !n) return R2D3C_EINVAL;
+  *n = (long long)c->nparam;
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_get_params(r2d3c_cnn* c, float* host) {
+  try {
+    if (!c || !host) throw Error(kEINVAL, "NULL argument");
+    cuda_check(cudaMemcpyAsync(host, c->wm, c->nparam * sizeof(float), cudaMemcpyDeviceToHost, c->st), "D2H");
+    cuda_check(cudaStreamSynchronize(c->st), "sync");
+  } catch (const Error& e) {
+    return fail(e);
+  }
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_set_params(r2d3c_cnn* c, const float* host) {
+  try {
+    if (!c || !host) throw Error(kEINVAL, "NULL argument");
+    cuda_check(cudaMemcpyAsync(c->wm, host, c->nparam * sizeof(float), cudaMemcpyHostToDevice, c->st), "H2D");
+    c->pack();
+    cuda_check(cudaStreamSynchronize(c->st), "sync");
+  } catch (const Error& e) {
+    return fail(e);
+  }
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_forward(r2d3c_cnn* c, const float* d_x, int batch, float* d_out) {
+  try {
+    if (!c || !d_x || !d_out) throw Error(kEINVAL, "NULL argument");
+    if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
+    c->forward(d_x, batch);
+    cuda_check(cudaMemcpyAsync(d_out, c->pre[kLayers - 1], (size_t)batch * c->H * c->W * 2 * sizeof(float),
+                               cudaMemcpyDeviceToDevice, c->st),
+               "D2D");
+    cuda_check(cudaStreamSynchronize(c->st), "sync");
+  } catch (const Error& e) {
+    return fail(e);
+  }
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_gradients(r2d3c_cnn* c, const float* d_x, const float* d_y, int batch, float* host_grad,
+                        double* loss) {
+  try {
+    if (!c || !d_x || !d_y) throw Error(kEINVAL, "NULL argument");
+    if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
+    c->forward(d_x, batch);
+    const double l = c->backward(d_y, batch);
+    if (loss) *loss = l;
+    if (host_grad) {
+      cuda_check(cudaMemcpyAsync(host_grad, c->grad, c->nparam * sizeof(float), cudaMemcpyDeviceToHost, c->st),
+                 "D2H");
+      cuda_check(cudaStreamSynchronize(c->st), "sync");
+    }
+  } catch (const Error& e) {
+    return fail(e);
+  }
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_train_step(r2d3c_cnn* c, const float* d_x, const float* d_y, int batch, float lr, double* loss) {
+  try {
+    if (!c || !d_x || !d_y) throw Error(kEINVAL, "NULL argument");
+    if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
+    c->forward(d_x, batch);
+    const double l = c->backward(d_y, batch);
+    c->adam(lr);
+    cuda_check(cudaStreamSynchronize(c->st), "sync");
+    if (loss) *loss = l;
+  } catch (const Error& e) {
+    return fail(e);
+  }
+  return R2D3C_OK;
+}
+
+}  // extern "C"
