@@ -219,6 +219,22 @@ int r2d3c_cnn_gradients(r2d3c_cnn* cnn, const float* d_x, const float* d_y, int 
                         double* loss);
 /* forward, backward and one Adam step (beta 0.9/0.999, eps 1e-8) */
 int r2d3c_cnn_train_step(r2d3c_cnn* cnn, const float* d_x, const float* d_y, int batch, float lr, double* loss);
+/* per-channel standardisation applied inside the network: inputs are mapped
+   to (x - in_mean)/in_std, targets likewise, outputs back to physical units
+   (the loss is in standardised units); identity by default */
+int r2d3c_cnn_set_normalization(r2d3c_cnn* cnn, const float* in_mean, const float* in_std, const float* out_mean,
+                                const float* out_std);
+/* Closure data of a coarse run (device FP32 NHWC on its n x n grid): the 8
+   network inputs of its current state (omega, vz, d/dx and d/dy of psi,
+   omega, vz); a training sample from a finer run -- the coarse state is set
+   to the sharp spectral filter (k^2 <= (nc/3)^2) of the fine state and the
+   targets are the subgrid parts of the two brackets,
+   P_c([psi,-k^2 psi]_fine) - [psi_c,-k^2 psi_c] and P_c([psi,vz]_fine) - [psi_c,vz_c];
+   and the tendencies (physical [n][n][2]) that the following steps add to
+   the two brackets of the RK update (NULL switches them off). */
+int r2d3c_closure_inputs(r2d3c_ctx* ctx, float* d_x);
+int r2d3c_closure_sample(r2d3c_ctx* fine, r2d3c_ctx* coarse, float* d_x, float* d_y);
+int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t);
 
 /* ---- Level 2 operators (reference subroutines on host arrays) ---------- */
 /* derivk2 (pseudospec2D_Rot2D3C.f90:6-68) */

@@ -479,10 +479,12 @@ class Seeds:
 
 
 def rk_step(g: Grid, p: Params, ps, vz, fp, fz, dt: float, seeds: Seeds | None = None,
-            ord: int = 4):
+            ord: int = 4, tau5=None, tau6=None):
     """One low-storage RK step of order ``ord`` (Rot2D3C.para.f90:545-611)
     with semi-implicit divisor dissipation.  Returns the new (ps, vz) and,
-    for iflow=2, the last forcing (fp, fz)."""
+    for iflow=2, the last forcing (fp, fz).  ``tau5``/``tau6`` (spectral,
+    optional) are learned subgrid tendencies added to the two brackets (no
+    counterpart in the reference)."""
     C1 = ps.copy()
     C2 = vz.copy()
     m = (g.ka2 <= g.kmax) & (g.ka2 > g.tiny)
@@ -495,6 +497,9 @@ def rk_step(g: Grid, p: Params, ps, vz, fp, fz, dt: float, seeds: Seeds | None =
         C4 = laplak2(g, C1)                                # :571
         C5 = poisson(g, C1, C4)                            # :572
         C6 = poisson(g, C1, C2)                            # :573
+        if tau5 is not None:
+            C5 = C5 + tau5
+            C6 = C6 + tau6
         C3 = derivk2(g, C1, 2)                             # :575
         C4 = derivk2(g, C2, 2)                             # :576
         tmp1 = dt / float(o)                               # :581
@@ -528,3 +533,40 @@ def random_phase_field(g: Grid, kmin: float, kmax_shell: float, slope: float,
     r = c2r(g, c)
     a = r2c(g, r) / float(n) ** 2
     return np.where(shell, a, 0.0)
+
+
+# --------------------------------------------------------------------------
+# learned-closure data (no counterpart in the reference)
+# --------------------------------------------------------------------------
+def coarsen(gf: Grid, gc: Grid, a: np.ndarray) -> np.ndarray:
+    """Sharp spectral filter of a fine spectral field onto the coarse grid:
+    modes with kx^2 + ky^2 <= (nc/3)^2 kept, rescaled by (nc/nf)^2 (both
+    grids carry the unnormalised R2C scaling)."""
+    nf, nc = gf.n, gc.n
+    out = np.zeros(gc.shape_spec, dtype=np.complex128)
+    for i in range(nc // 2):
+        for j in range(nc):
+            ky = int(gc.ka[j])
+            if i * i + ky * ky <= gc.kmax:
+                out[i, j] = a[i, ky if ky >= 0 else nf + ky] * (nc / nf) ** 2
+    return out
+
+
+def closure_inputs(g: Grid, ps, vz) -> np.ndarray:
+    """[n, n, 8]: omega = k^2 psi, vz, d/dx and d/dy of psi, omega, vz in
+    physical units (C2R / n^2)."""
+    n2 = float(g.n) ** 2
+    om = -laplak2(g, ps)
+    fields = [om, derivk2(g, vz, 0), derivk2(g, ps, 1), derivk2(g, ps, 2), derivk2(g, om, 1),
+              derivk2(g, om, 2), derivk2(g, vz, 1), derivk2(g, vz, 2)]
+    return np.stack([c2r(g, f) / n2 for f in fields], axis=-1)
+
+
+def closure_targets(gf: Grid, gc: Grid, psf, vzf) -> np.ndarray:
+    """[nc, nc, 2]: P_c([psi,-k^2 psi]_f) - [psi_c,-k^2 psi_c] and
+    P_c([psi,vz]_f) - [psi_c,vz_c], physical units."""
+    psc, vzc = coarsen(gf, gc, psf), coarsen(gf, gc, vzf)
+    t5 = coarsen(gf, gc, poisson(gf, psf, laplak2(gf, psf))) - poisson(gc, psc, laplak2(gc, psc))
+    t6 = coarsen(gf, gc, poisson(gf, psf, vzf)) - poisson(gc, psc, vzc)
+    n2 = float(gc.n) ** 2
+    return np.stack([c2r(gc, t5) / n2, c2r(gc, t6) / n2], axis=-1)

@@ -109,6 +109,11 @@ SIGNATURES = {
     "r2d3c_cnn_forward": (C.c_int, [_P, _P, C.c_int, _P]),
     "r2d3c_cnn_gradients": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(C.c_float), _D]),
     "r2d3c_cnn_train_step": (C.c_int, [_P, _P, _P, C.c_int, C.c_float, _D]),
+    "r2d3c_cnn_set_normalization": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                              C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "r2d3c_closure_inputs": (C.c_int, [_P, _P]),
+    "r2d3c_closure_sample": (C.c_int, [_P, _P, _P, _P]),
+    "r2d3c_closure_set_tendency": (C.c_int, [_P, _P]),
     "r2d3c_derivk2": (C.c_int, [_P, _D, _D, C.c_int]),
     "r2d3c_laplak2": (C.c_int, [_P, _D, _D]),
     "r2d3c_inv_laplak2": (C.c_int, [_P, _D, _D]),

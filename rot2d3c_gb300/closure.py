@@ -38,6 +38,11 @@ class CNN:
         assert p.size == self.nparams
         check(load().r2d3c_cnn_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))), "cnn_set_params")
 
+    def set_normalization(self, in_mean, in_std, out_mean, out_std) -> None:
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (in_mean, in_std, out_mean, out_std)]
+        ptrs = [a.ctypes.data_as(C.POINTER(C.c_float)) for a in arrs]
+        check(load().r2d3c_cnn_set_normalization(self._h, *ptrs), "cnn_set_normalization")
+
     def forward(self, x, batch: int, out) -> None:
         check(load().r2d3c_cnn_forward(self._h, _ptr(x), batch, _ptr(out)), "cnn_forward")
 
@@ -63,3 +68,19 @@ class CNN:
             self.destroy()
         except Exception:
             pass
+
+
+def closure_inputs(ctx, d_x) -> None:
+    """The 8 network inputs of ctx's current state into d_x ([n, n, 8] FP32)."""
+    check(load().r2d3c_closure_inputs(ctx._h, _ptr(d_x)), "closure_inputs")
+
+
+def closure_sample(fine, coarse, d_x, d_y) -> None:
+    """Filter fine's state onto coarse; inputs and subgrid targets of it."""
+    check(load().r2d3c_closure_sample(fine._h, coarse._h, _ptr(d_x), _ptr(d_y)), "closure_sample")
+
+
+def set_tendency(ctx, d_t) -> None:
+    """Subgrid tendencies ([n, n, 2] FP32, physical) added to the brackets of
+    the following steps of ctx; None switches them off."""
+    check(load().r2d3c_closure_set_tendency(ctx._h, None if d_t is None else _ptr(d_t)), "closure_set_tendency")

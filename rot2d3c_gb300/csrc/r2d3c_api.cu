@@ -940,6 +940,33 @@ int r2d3c_fp64_fma_peak(double* tflops) {
   API_END
 }
 
+// ---------------------------------------------------------------- closure
+int r2d3c_closure_inputs(r2d3c_ctx* ctx, float* d_x) {
+  API_BEGIN
+  REQUIRE(ctx && d_x, "NULL argument");
+  ctx->eng->closure_inputs(d_x);
+  API_END
+}
+
+int r2d3c_closure_sample(r2d3c_ctx* fine, r2d3c_ctx* coarse, float* d_x, float* d_y) {
+  API_BEGIN
+  REQUIRE(fine && coarse && d_x && d_y, "NULL argument");
+  REQUIRE(fine->p.n > coarse->p.n, "the fine grid must be larger than the coarse grid");
+  IEngine* c = coarse->eng.get();
+  c->coarsen_from(fine->eng.get(), P_PS, P_PS);
+  c->coarsen_from(fine->eng.get(), P_VZ, P_VZ);
+  c->closure_inputs(d_x);
+  c->closure_targets(fine->eng.get(), d_y);
+  API_END
+}
+
+int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  ctx->eng->set_closure(d_t);
+  API_END
+}
+
 int r2d3c_dev_ptr(r2d3c_ctx* ctx, int which, void** ptr) {
   API_BEGIN
   REQUIRE(ctx && ptr, "NULL argument");

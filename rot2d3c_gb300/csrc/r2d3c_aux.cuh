@@ -460,4 +460,50 @@ __global__ void k_ci_rescale(const cpx<T>* __restrict__ src, cpx<T>* __restrict_
   if (mirror[e] >= 0) dst[mirror[e]] = mkc<T>((T)vx, (T)(-vy));
 }
 
+// ---------------------------------------------------------------------------
+// learned-closure plumbing
+// ---------------------------------------------------------------------------
+// sharp spectral filter: coarse[kx][ky] = fine[kx][ky] * (nc/nf)^2 for
+// kx^2 + ky^2 <= kmaxi of the coarse grid, else 0
+template <typename T>
+__global__ void k_coarsen(const cpx<T>* __restrict__ fine, int nf, cpx<T>* __restrict__ coarse, DevGrid gc,
+                          double scale) {
+  const size_t total = (size_t)gc.nh * gc.n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / gc.n), j = (int)(idx % gc.n);
+    const int ky = ky_of(j, gc.n);
+    const int k2 = i * i + ky * ky;
+    cpx<T> v = czero<T>();
+    if (i < gc.n / 2 && k2 <= gc.kmaxi) {
+      const cpx<T> f = fine[(size_t)i * nf + (ky >= 0 ? ky : nf + ky)];
+      v = mkc<T>((T)(f.x * scale), (T)(f.y * scale));
+    }
+    coarse[idx] = v;
+  }
+}
+
+// c = a - b on spectral planes
+template <typename T>
+__global__ void k_spec_sub(const cpx<T>* __restrict__ a, const cpx<T>* __restrict__ b, cpx<T>* __restrict__ c,
+                           size_t total) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+    c[i] = mkc<T>(a[i].x - b[i].x, a[i].y - b[i].y);
+}
+
+// out[p*nch + ch] = r[p] * s  (real plane -> one channel of an FP32 NHWC tensor)
+template <typename T>
+__global__ void k_to_channel(const T* __restrict__ r, size_t count, double s, float* __restrict__ out, int nch,
+                             int ch) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < count; p += (size_t)gridDim.x * blockDim.x)
+    out[p * nch + ch] = (float)((double)r[p] * s);
+}
+
+// r[p] = in[p*nch + ch]
+template <typename T>
+__global__ void k_from_channel(const float* __restrict__ in, int nch, int ch, size_t count, T* __restrict__ r) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < count; p += (size_t)gridDim.x * blockDim.x)
+    r[p] = (T)in[p * nch + ch];
+}
+
 }  // namespace r2d3c

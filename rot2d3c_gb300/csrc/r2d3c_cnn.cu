@@ -259,7 +259,8 @@ __global__ void k_gelu_back(const bf16* __restrict__ da, const float* __restrict
 // MSE loss of the 2 output channels against the target; dY of the last
 // layer (padded to 16 channels, zero beyond 2) and per-CTA loss partials
 __global__ void k_mse(const float* __restrict__ out, const float* __restrict__ tgt, size_t npix, float scale,
-                      bf16* __restrict__ dy, float* __restrict__ lpart) {
+                      const float* __restrict__ tmean, const float* __restrict__ tsd, bf16* __restrict__ dy,
+                      float* __restrict__ lpart) {
   __shared__ float red[256];
   float s = 0.f;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npix; p += (size_t)gridDim.x * blockDim.x) {
@@ -267,7 +268,7 @@ __global__ void k_mse(const float* __restrict__ out, const float* __restrict__ t
     for (int c = 0; c < 16; ++c) {
       float g = 0.f;
       if (c < 2) {
-        const float d = out[p * 2 + c] - tgt[p * 2 + c];
+        const float d = out[p * 2 + c] - (tgt[p * 2 + c] - tmean[c]) / tsd[c];
         s += d * d;
         g = 2.f * d * scale;
       }
@@ -319,12 +320,23 @@ __global__ void k_unpad_wgrad(const float* __restrict__ gp, int cin, int cout, i
   g[i] = gp[((size_t)tap * cinp + ci) * coutp + co];
 }
 
-// FP32 NHWC [npix][c] -> bf16 NHWC [npix][cp] (zero padding channels)
-__global__ void k_to_bf16(const float* __restrict__ x, size_t npix, int c, int cp, bf16* __restrict__ out) {
+// FP32 NHWC [npix][c] -> bf16 NHWC [npix][cp], (x - mean[ch]) / std[ch],
+// zero padding channels
+__global__ void k_to_bf16(const float* __restrict__ x, size_t npix, int c, int cp, const float* __restrict__ mean,
+                          const float* __restrict__ sd, bf16* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix * cp; i += (size_t)gridDim.x * blockDim.x) {
     const size_t p = i / cp;
     const int ch = (int)(i % cp);
-    out[i] = __float2bfloat16_rn(ch < c ? x[p * c + ch] : 0.f);
+    out[i] = __float2bfloat16_rn(ch < c ? (x[p * c + ch] - mean[ch]) / sd[ch] : 0.f);
+  }
+}
+
+// out = y * std[ch] + mean[ch] for the 2 output channels
+__global__ void k_denorm(const float* __restrict__ y, size_t npix, const float* __restrict__ mean,
+                         const float* __restrict__ sd, float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix * 2; i += (size_t)gridDim.x * blockDim.x) {
+    const int ch = (int)(i & 1);
+    out[i] = y[i] * sd[ch] + mean[ch];
   }
 }
 
@@ -362,6 +374,7 @@ struct r2d3c_cnn {
   bf16 *dA = nullptr, *dY = nullptr;
   float* part = nullptr;
   float* lpart = nullptr;
+  float* norm = nullptr;  // in mean[8], in std[8], out mean[2], out std[2]
   int nparts = 304;
   long long step = 0;
   std::vector<void*> owned;
@@ -400,7 +413,7 @@ struct r2d3c_cnn {
   // forward of a batch of B inputs (f32 NHWC 8 ch) -> pre[kLayers-1] (f32 NHWC 2 ch)
   void forward(const float* x, int B) {
     const size_t npix = (size_t)B * H * W;
-    k_to_bf16<<<1024, 256, 0, st>>>(x, npix, 8, 16, act[0]);
+    k_to_bf16<<<1024, 256, 0, st>>>(x, npix, 8, 16, norm, norm + 8, act[0]);
     cuda_check(cudaGetLastError(), "k_to_bf16");
     for (int l = 0; l < kLayers; ++l) {
       const bool last = l == kLayers - 1;
@@ -412,7 +425,7 @@ struct r2d3c_cnn {
   double backward(const float* tgt, int B) {
     const size_t npix = (size_t)B * H * W;
     const float scale = 1.0f / (float)(npix * 2);
-    k_mse<<<256, 256, 0, st>>>(pre[kLayers - 1], tgt, npix, scale, dY, lpart);
+    k_mse<<<256, 256, 0, st>>>(pre[kLayers - 1], tgt, npix, scale, norm + 16, norm + 18, dY, lpart);
     cuda_check(cudaGetLastError(), "k_mse");
     for (int l = kLayers - 1; l >= 0; --l) {
       const Layer& ly = L[l];
@@ -521,6 +534,9 @@ int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** out) {
     c->dY = c->alloc<bf16>(npix * 32);  // dL/dy of the current layer (<= 32 channels)
     c->part = c->alloc<float>((size_t)(c->nparts + 1) * 9 * 32 * 32);
     c->lpart = c->alloc<float>(256);
+    c->norm = c->alloc<float>(20);
+    const float ident[20] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 1, 1};
+    cuda_check(cudaMemcpyAsync(c->norm, ident, sizeof(ident), cudaMemcpyHostToDevice, c->st), "H2D");
     c->pack();
     cuda_check(cudaStreamSynchronize(c->st), "sync");
     *out = c.release();
@@ -567,14 +583,37 @@ int r2d3c_cnn_set_params(r2d3c_cnn* c, const float* host) {
   return R2D3C_OK;
 }
 
+int r2d3c_cnn_set_normalization(r2d3c_cnn* c, const float* in_mean, const float* in_std, const float* out_mean,
+                                const float* out_std) {
+  try {
+    if (!c || !in_mean || !in_std || !out_mean || !out_std) throw Error(kEINVAL, "NULL argument");
+    float h[20];
+    for (int i = 0; i < 8; ++i) {
+      if (!(in_std[i] > 0.f)) throw Error(kEINVAL, "standard deviations must be positive");
+      h[i] = in_mean[i];
+      h[8 + i] = in_std[i];
+    }
+    for (int i = 0; i < 2; ++i) {
+      if (!(out_std[i] > 0.f)) throw Error(kEINVAL, "standard deviations must be positive");
+      h[16 + i] = out_mean[i];
+      h[18 + i] = out_std[i];
+    }
+    cuda_check(cudaMemcpyAsync(c->norm, h, sizeof(h), cudaMemcpyHostToDevice, c->st), "H2D");
+    cuda_check(cudaStreamSynchronize(c->st), "sync");
+  } catch (const Error& e) {
+    return fail(e);
+  }
+  return R2D3C_OK;
+}
+
 int r2d3c_cnn_forward(r2d3c_cnn* c, const float* d_x, int batch, float* d_out) {
   try {
     if (!c || !d_x || !d_out) throw Error(kEINVAL, "NULL argument");
     if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
     c->forward(d_x, batch);
-    cuda_check(cudaMemcpyAsync(d_out, c->pre[kLayers - 1], (size_t)batch * c->H * c->W * 2 * sizeof(float),
-                               cudaMemcpyDeviceToDevice, c->st),
-               "D2D");
+    k_denorm<<<512, 256, 0, c->st>>>(c->pre[kLayers - 1], (size_t)batch * c->H * c->W, c->norm + 16, c->norm + 18,
+                                     d_out);
+    cuda_check(cudaGetLastError(), "k_denorm");
     cuda_check(cudaStreamSynchronize(c->st), "sync");
   } catch (const Error& e) {
     return fail(e);

@@ -25,7 +25,7 @@ constexpr int kOK = 0, kEINVAL = -1, kECUDA = -2, kENOMEM = -3, kETIMEOUT = -4, 
 void cuda_check(cudaError_t e, const char* what);
 
 // Spectral planes: complex [kx][ky], (n/2+1) x n.
-enum Plane : int { P_PS = 0, P_VZ, P_FP, P_FZ, P_C1, P_C2, P_W1, P_W2, P_B5, P_B6, P_COUNT };
+enum Plane : int { P_PS = 0, P_VZ, P_FP, P_FZ, P_C1, P_C2, P_W1, P_W2, P_B5, P_B6, P_T5, P_T6, P_COUNT };
 // Real planes: [y][x], n x n.
 enum RPlane : int { R_1 = 0, R_2, R_3, R_COUNT };
 
@@ -98,6 +98,16 @@ class IEngine {
   // every run on stream() while the capture is open.
   virtual void prepare_steps(double cfl) = 0;
   virtual void enqueue_steps(bool cfl_mode) = 0;
+
+  // learned closure (coarse runs): 8 CNN input channels of the current state
+  // (physical, FP32 NHWC [n][n][8]); the subgrid targets against a finer run
+  // (FP32 NHWC [n][n][2]); the tendencies added to the two brackets by the
+  // following steps (physical FP32 [n][n][2]; null switches them off)
+  virtual void closure_inputs(float* d_x) = 0;
+  virtual void brackets() = 0;  // [psi,-k^2 psi] -> P_B5, [psi,vz] -> P_B6 (full plane)
+  virtual void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) = 0;
+  virtual void closure_targets(IEngine* fine, float* d_y) = 0;
+  virtual void set_closure(const float* d_t) = 0;
   virtual void rand_force(const RandForceHost f[2]) = 0;
   // One RK4 step.  cfl_mode: dt from the CFL condition of the current state
   // (fused into the first substep), else the dt already set.  add_time:

@@ -438,7 +438,7 @@ class EngineT final : public IEngine {
       sync();  // seq goes out of scope
     }
     upload_coefs(mc, cfl);
-    GraphKey key{cfl_mode, rf != nullptr};
+    GraphKey key{cfl_mode, rf != nullptr, closure_on_};
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
@@ -535,10 +535,76 @@ class EngineT final : public IEngine {
   // The captured step depends only on these; coefficients and dt live in
   // device arrays read by the kernels, so changing them needs no recapture.
   struct GraphKey {
-    bool cfl_mode = false, rf = false;
-    bool same(const GraphKey& o) const { return cfl_mode == o.cfl_mode && rf == o.rf; }
+    bool cfl_mode = false, rf = false, closure = false;
+    bool same(const GraphKey& o) const {
+      return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure;
+    }
   };
   static bool batched(int p) { return p <= P_C2; }  // ps, vz, fp, fz, c1, c2
+
+ public:
+  void closure_inputs(float* d_x) override {
+    const size_t cnt = (size_t)n_ * n_;
+    const double s = 1.0 / ((double)n_ * n_);
+    // omega = -lap psi = k^2 psi: -(laplak2 psi); vz; d/dx, d/dy of psi, omega, vz
+    struct Ch { int src, op1, op2; double sign; };
+    const Ch ch[8] = {{P_PS, OP_LAPLA, -1, -1.0}, {P_VZ, OP_COPY_MASK, -1, 1.0},
+                      {P_PS, OP_DERIV_X, -1, 1.0}, {P_PS, OP_DERIV_Y, -1, 1.0},
+                      {P_PS, OP_LAPLA, OP_DERIV_X, -1.0}, {P_PS, OP_LAPLA, OP_DERIV_Y, -1.0},
+                      {P_VZ, OP_DERIV_X, -1, 1.0}, {P_VZ, OP_DERIV_Y, -1, 1.0}};
+    for (int c = 0; c < 8; ++c) {
+      specop(ch[c].src, P_W2, ch[c].op1, 0.0);
+      if (ch[c].op2 >= 0) specop(P_W2, P_W1, ch[c].op2, 0.0);
+      c2r(ch[c].op2 >= 0 ? P_W1 : P_W2, R_1, nullptr, nullptr);
+      k_to_channel<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_1], cnt, ch[c].sign * s, d_x, 8, c);
+      post("k_to_channel");
+    }
+    sync();
+  }
+  void brackets() override { brackets_full(); }
+  void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) override {
+    if (fine->precision() != precision() || fine->n() <= n_) throw Error(kEINVAL, "coarsen: finer grid of the same precision");
+    const double r = (double)n_ / (double)fine->n();
+    k_coarsen<T><<<elem_blocks(S_), 256, 0, st_>>>(static_cast<const cpx<T>*>(fine->plane_ptr(fine_plane)), fine->n(),
+                                                   planes_[dst_plane], gd_, r * r);
+    post("k_coarsen");
+  }
+  void closure_targets(IEngine* fine, float* d_y) override {
+    // tau = P_c([.,.]_fine) - [.,.]_coarse for both brackets, in physical space
+    fine->brackets();
+    fine->sync();
+    brackets();
+    const size_t cnt = (size_t)n_ * n_;
+    const double s = 1.0 / ((double)n_ * n_);
+    for (int c = 0; c < 2; ++c) {
+      coarsen_from(fine, c == 0 ? P_B5 : P_B6, P_W1);
+      k_spec_sub<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[P_W1], planes_[c == 0 ? P_B5 : P_B6], planes_[P_W1], S_);
+      post("k_spec_sub");
+      c2r(P_W1, R_1, nullptr, nullptr);
+      k_to_channel<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_1], cnt, s, d_y, 2, c);
+      post("k_to_channel");
+    }
+    sync();
+  }
+  void set_closure(const float* d_t) override {
+    if (!d_t) {
+      closure_on_ = false;
+      return;
+    }
+    if (nb_ != 1) throw Error(kEINVAL, "the closure is a single-run feature");
+    const size_t cnt = (size_t)n_ * n_;
+    for (int c = 0; c < 2; ++c) {
+      k_from_channel<T><<<elem_blocks(cnt), 256, 0, st_>>>(d_t, 2, c, cnt, rplanes_[R_1]);
+      post("k_from_channel");
+      r2c(R_1, c == 0 ? P_T5 : P_T6);
+    }
+    // the tendency planes are fixed buffers: a captured step keyed on
+    // closure_on_ stays valid across calls
+    closure_on_ = true;
+    sync();
+  }
+
+ private:
   // per-run coefficient arrays: nb == 1 takes mc, a batch its run coefficients
   void upload_coefs(const ModelCoef& mc, double cfl) {
     if (nb_ == 1) coefs_.assign(1, mc);
@@ -803,7 +869,9 @@ class EngineT final : public IEngine {
       const int groups = (gd_.M + NT - 1) / NT;
       const dim3 grid((groups + C::G - 1) / C::G, nb);
       k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ], pbase_[P_FP],
-                                           pbase_[P_FZ], c1out, c2out, gd_, d_sc_, scal_base_, o, tw_, batch());
+                                           pbase_[P_FZ], c1out, c2out, gd_, d_sc_, scal_base_, o, tw_, batch(),
+                                           closure_on_ ? pbase_[P_T5] : nullptr,
+                                           closure_on_ ? pbase_[P_T6] : nullptr);
       post("k_passC");
     });
   }
@@ -848,6 +916,7 @@ class EngineT final : public IEngine {
   int n_, dev_;
   bool full_;
   int nb_ = 1, run_ = 0;
+  bool closure_on_ = false;
   cpx<T>* pbase_[P_COUNT] = {};
   double* scal_base_ = nullptr;
   unsigned long long* enc_base_ = nullptr;

@@ -565,7 +565,8 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         const cpx<T>* ps, const cpx<T>* vz, const cpx<T>* __restrict__ fp,
         const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out, DevGrid gd,
         const StepCoef* __restrict__ scs, const double* __restrict__ scal, int o,
-        const tw_t<T>* __restrict__ tw, Batch bs) {
+        const tw_t<T>* __restrict__ tw, Batch bs, const cpx<T>* __restrict__ tau5,
+        const cpx<T>* __restrict__ tau6) {
   constexpr int NT = PassNT<T, N>::value;
   using PS = PassSmem<T, N>;
   constexpr bool HOLD = PS::HOLD;
@@ -646,8 +647,15 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
       cpx<T> c5;
       if constexpr (HOLD) c5 = hold[t * N + j];
       else c5 = c5r[t][q];
-      rk_update<T>(c5, v[t][q], (size_t)col * N + j, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp,
-                   fz, c1out, c2out, sc, tmp1, gd.kmaxi);
+      cpx<T> c6 = v[t][q];
+      const size_t idx = (size_t)col * N + j;
+      if (tau5) {  // learned subgrid tendencies of the two brackets
+        const cpx<T> a = tau5[idx], b = tau6[idx];
+        c5 = mkc<T>(c5.x + a.x, c5.y + a.y);
+        c6 = mkc<T>(c6.x + b.x, c6.y + b.y);
+      }
+      rk_update<T>(c5, c6, idx, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp, fz, c1out, c2out, sc, tmp1,
+                   gd.kmaxi);
     }
   }
 }

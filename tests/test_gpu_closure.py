@@ -1,0 +1,80 @@
+"""The learned-closure data path against the oracle: sharp spectral filter of
+a fine run onto a coarse grid, the 8 network inputs, the subgrid bracket
+targets, and the RK step with tendencies added to the brackets."""
+import numpy as np
+import pytest
+
+from oracle import rot2d3c_oracle as O
+from tests._helpers import params, random_forcing, random_state, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 2e-5)])
+def test_closure_sample_matches_oracle(gpu, prec, tol):
+    import torch
+    from rot2d3c_gb300.closure import closure_sample
+    nf, nc = 64, 32
+    gf, gc = O.Grid(nf), O.Grid(nc)
+    _, cpf = params(nf, iflow=0)
+    _, cpc = params(nc, iflow=0)
+    _, psf, vzf = random_state(nf, 5, amp=4.0)
+    fine, coarse = gpu.Context(cpf, prec), gpu.Context(cpc, prec)
+    fine.set_state(psf, vzf)
+    dx = torch.zeros((nc, nc, 8), dtype=torch.float32, device="cuda")
+    dy = torch.zeros((nc, nc, 2), dtype=torch.float32, device="cuda")
+    closure_sample(fine, coarse, dx, dy)
+    a, b = coarse.get_state()
+    assert rel_l2(a, O.coarsen(gf, gc, psf)) < tol and rel_l2(b, O.coarsen(gf, gc, vzf)) < tol
+    x = O.closure_inputs(gc, O.coarsen(gf, gc, psf), O.coarsen(gf, gc, vzf))
+    t = O.closure_targets(gf, gc, psf, vzf)
+    xs, ts = dx.cpu().numpy(), dy.cpu().numpy()
+    ftol = max(tol, 2e-6)  # channels are stored in FP32
+    for c in range(8):
+        assert rel_l2(xs[..., c], x[..., c]) < ftol, c
+    for c in range(2):
+        assert rel_l2(ts[..., c], t[..., c]) < 10 * ftol, c
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 1e-5)])
+def test_step_with_subgrid_tendencies(gpu, prec, tol):
+    import torch
+    from rot2d3c_gb300.closure import set_tendency
+    n = 32
+    p, cp = params(n, omega=1.0, nu=1e-3, hnu=0.1, nuv=1e-3, hnuv=0.1, iflow=0)
+    g, ps, vz = random_state(n, 8, amp=10.0)
+    fp, fz = random_forcing(g, 9)
+    rng = np.random.default_rng(2)
+    t = np.stack([O.c2r(g, O.random_phase_field(g, 1, 10, -1.0, rng)) for _ in range(2)], axis=-1)
+    t = (t / n**2 * 1e3).astype(np.float32)
+    c = gpu.Context(cp, prec)
+    c.set_state(ps, vz)
+    c.set_forcing(fp, fz)
+    set_tendency(c, torch.from_numpy(t).cuda())
+    c.step(1e-3)
+    c.advance(2, gpu.DT_FIXED, 1e-3)
+    tau5 = O.r2c(g, t[..., 0].astype(np.float64))
+    tau6 = O.r2c(g, t[..., 1].astype(np.float64))
+    for _ in range(3):
+        ps, vz, fp, fz = O.rk_step(g, p, ps, vz, fp, fz, 1e-3, tau5=tau5, tau6=tau6)
+    a, b = c.get_state()
+    assert rel_l2(a, ps) < tol and rel_l2(b, vz) < tol
+    set_tendency(c, None)
+
+
+def test_cnn_normalisation_maps_units(gpu):
+    import torch
+    from oracle import cnn_oracle as CO
+    from rot2d3c_gb300.closure import CNN
+    H, W = 8, 16
+    net = CNN(H, W, 1, seed=4)
+    rng = np.random.default_rng(1)
+    im, isd = rng.standard_normal(8).astype(np.float32), rng.uniform(0.5, 2, 8).astype(np.float32)
+    om, osd = rng.standard_normal(2).astype(np.float32), rng.uniform(0.5, 2, 2).astype(np.float32)
+    net.set_normalization(im, isd, om, osd)
+    x = rng.standard_normal((1, H, W, 8)).astype(np.float32) * 3
+    out = torch.empty((1, H, W, 2), dtype=torch.float32, device="cuda")
+    net.forward(torch.from_numpy(x).cuda(), 1, out)
+    ref, _, _ = CO.forward(net.get_params().astype(np.float64), (x - im) / isd)
+    ref = ref * osd + om
+    assert np.linalg.norm(out.cpu().numpy() - ref) <= 1e-2 * np.linalg.norm(ref)
