@@ -854,10 +854,22 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       constexpr int NR = PassNT<T, N>::value;
       using C = Cfg<T, N, NR>;
-      auto k = k_passB<T, N, CFL>;
-      const dim3 grid((N / NR + C::G - 1) / C::G, nb);
-      k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
-      post("k_passB");
+      if constexpr (kPipeB<T, N>) {
+        // persistent: about as many CTAs as fit on the device at once
+        constexpr int EP = PipeB<N>::E;
+        static_assert(EP == PassAE<T, N>::value || EP == Cfg<T, N>::E, "pass B radix has a twiddle table");
+        const tw_t<T>* twp = EP == PassAE<T, N>::value ? tw_a_ : tw_;
+        const int per_run = std::max(1, std::min(N / 2, (pipeb_ctas_ + nb - 1) / nb));
+        auto k = k_passB_pipe<N, CFL>;
+        k<<<dim3(per_run, nb), PipeB<N>::THREADS, PipeB<N>::smem(gd_.M), st_>>>(tf, pb, kxo, gd_, inv4, twp,
+                                                                                  enc_base_, batch());
+        post("k_passB_pipe");
+      } else {
+        auto k = k_passB<T, N, CFL>;
+        const dim3 grid((N / NR + C::G - 1) / C::G, nb);
+        k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
+        post("k_passB");
+      }
     });
   }
   void launch_passC(const cpx<T>* c1in, const cpx<T>* c2in, cpx<T>* c1out, cpx<T>* c2out, int o, int nb) {
@@ -892,6 +904,19 @@ class EngineT final : public IEngine {
       set_smem_attr(k_passB<T, N, true>, smh);
       set_smem_attr(k_passB<T, N, false>, smh);
       set_smem_attr(k_passC<T, N>, smh);
+      if constexpr (kPipeB<T, N>) {
+        const size_t smp = PipeB<N>::smem(gd_.M);
+        set_smem_attr(k_passB_pipe<N, true>, smp);
+        set_smem_attr(k_passB_pipe<N, false>, smp);
+        int per_sm = 0, sms = 0, dev = 0;
+        cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_passB_pipe<N, true>,
+                                                                 PipeB<N>::THREADS, smp),
+                   "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+        if (per_sm < 1) throw Error(kEINVAL, "pass B pipeline does not fit on this device");
+        pipeb_ctas_ = per_sm * sms;
+      }
     });
   }
 
@@ -917,6 +942,7 @@ class EngineT final : public IEngine {
   bool full_;
   int nb_ = 1, run_ = 0;
   bool closure_on_ = false;
+  int pipeb_ctas_ = 0;  // resident CTAs of the pipelined pass B (whole device)
   cpx<T>* pbase_[P_COUNT] = {};
   double* scal_base_ = nullptr;
   unsigned long long* enc_base_ = nullptr;

@@ -110,6 +110,14 @@ __host__ __device__ __forceinline__ size_t mix_idx(int kx, int y, int MX) {
 // ky value of row index j (Rot2D3C.para.f90:220-223)
 __device__ __forceinline__ int ky_of(int j, int n) { return j < (n >> 1) ? j : j - n; }
 
+// x through an opaque move: the compiler cannot treat the result as equal
+// to x, so values derived from it are not hoisted out of a loop
+__device__ __forceinline__ int opaque(int x) {
+  int r;
+  asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(x));
+  return r;
+}
+
 template <typename T>
 __device__ __forceinline__ cpx<T> czero() {
   return mkc<T>((T)0, (T)0);
@@ -525,38 +533,296 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
 }
 
 // --------------------------------------------------------------------------
+// Pass B, FP32 pair-tiled grids with one transform group per CTA (n = 2048,
+// 4096): persistent CTAs that stage each row pair's mixed-plane inputs in
+// shared memory with asynchronous copies (cp.async, 16 bytes per thread and
+// instruction) one plane pair ahead of the transform that needs it, so that
+// the global loads of pairs 2 and 3 and of the next row pair's pair 1 overlap
+// the x-transforms instead of stalling them.  Same arithmetic, in the same
+// order, as k_passB: results are bit-identical.
+//
+// Shared memory: the transform buffers (2 x SMEM_ELEMS), the held z1
+// (2 x N) and two staging buffers S0, S1 of one plane pair each (2 x M
+// float4: the retained kx < M of rows y0, y0+1 of two planes).  Pipeline of
+// one row pair (S0: pairs 1 and 3, S1: pair 2, then the first bracket p1):
+//   wait pair 1 -> read it (S0) -> copy pair 3 into S0 -> x-IFFT z1
+//   wait pair 2 -> read it (S1) -> x-IFFT z2 -> p1 into S1
+//   wait pair 3 -> read it (S0) -> copy the next row pair's pair 1 into S0
+//   -> x-IFFT z3 -> products -> x-FFT -> copy the next row pair's pair 2
+//   into S1 -> Hermitian split -> stores
+// cp.async.wait_group is a hardware wait on the thread's own copies (no spin
+// loop); a barrier after it makes every thread's copies visible to all.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory");
+}
+
+// One plane pair of row pair rp into dst (plane a at [0, M), plane b at
+// [M, 2M)) as one commit group; `on` false commits an empty group so that the
+// group count stays the same on every path.
+template <int THREADS>
+__device__ __forceinline__ void stage_plane_pair(float4* dst, const float4* __restrict__ pa,
+                                                 const float4* __restrict__ pb, int M, bool on) {
+  if (on) {
+    for (int i = threadIdx.x; i < 2 * M; i += THREADS) cp_async16(dst + i, i < M ? pa + i : pb + (i - M));
+  }
+  cp_async_commit();
+}
+
+// Launch shape of the pipelined pass B: G groups of TPF = N/E threads, each
+// group carrying NT of the row pair's two rows (G * NT == 2).  Radix 8 with
+// both rows in one group measured fastest at n = 4096 (radix 16 with one row
+// per group: 5% slower).
+template <int N>
+struct PipeB {
+  static constexpr int E = 8;
+  static constexpr int NT = 2;
+  static constexpr int G = 2 / NT;
+  using F = BlockFFT<float, N, E, NT>;
+  static constexpr int TPF = N / E;
+  static constexpr int THREADS = G * TPF;
+  static constexpr int MINB = N >= 4096 ? 1 : 2;  // CTAs per SM (shared memory allows one at n = 4096)
+  // dynamic shared memory for M retained columns: transform buffers, held z1,
+  // two staging buffers
+  static size_t smem(int M) {
+    return (size_t)G * NT * F::SMEM_ELEMS * sizeof(float2) + (size_t)2 * N * sizeof(float2) +
+           (size_t)4 * M * sizeof(float4);
+  }
+};
+
+// pass B runs as k_passB_pipe where it applies
+template <typename T, int N>
+constexpr bool kPipeB = sizeof(T) == 4 && PassNT<T, N>::value == 2 && PipeB<N>::THREADS >= 256 &&
+                        PipeB<N>::THREADS <= 512;
+
+// Row t (0/1) of the staged pair at column kk: S holds float4 (row 0, row 1).
+__device__ __forceinline__ float2 staged_row(const float4* S, int idx, int t) {
+  return reinterpret_cast<const float2*>(S)[2 * idx + t];
+}
+
+template <int N, bool CFL>
+__global__ void __launch_bounds__(PipeB<N>::THREADS, PipeB<N>::MINB)
+k_passB_pipe(const float2* __restrict__ tf, float2* __restrict__ pb, int kxo, DevGrid gd, float inv_n4,
+             const float4* __restrict__ tw, unsigned long long* __restrict__ cfl_enc, Batch bs) {
+  using T = float;
+  using PB = PipeB<N>;
+  constexpr int NT = PB::NT, E = PB::E, TPF = PB::TPF, THREADS = PB::THREADS;
+  using F = typename PB::F;
+  constexpr int NRP = N / 2;  // row pairs
+  tf += blockIdx.y * bs.tf;
+  pb += blockIdx.y * bs.pb;
+  cfl_enc += blockIdx.y * kScalStride;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / TPF, lane = threadIdx.x % TPF;
+  const int r0 = g * NT;  // first row of the pair carried by this group
+  cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
+  cpx<T>* hold = smbase_ + (size_t)PB::G * NT * F::SMEM_ELEMS + (size_t)r0 * N;
+  const int M = gd.M;
+  float4* S0 = reinterpret_cast<float4*>(smbase_ + (size_t)PB::G * NT * F::SMEM_ELEMS + (size_t)2 * N);
+  float4* S1 = S0 + 2 * M;
+  float* P1 = reinterpret_cast<float*>(S1) + (size_t)r0 * N;  // p1 (after pair 2 is read)
+  // plane p, row pair rp: P + p * pl4 + rp * M (float4 = two rows of one column)
+  const float4* P = reinterpret_cast<const float4*>(tf);
+  const size_t pl4 = (size_t)M * NRP;
+  const size_t oplane = (size_t)gd.nh * N;
+  const T h = (T)0.5;
+  // packed spectrum Z[k] of the staged pair for this group's rows
+  auto load_z = [&](const float4* S, cpx<T> (&v)[NT][E]) {
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int k = lane + q * TPF;
+      if (k < M || k > N - M) {
+        const int kk = k < M ? k : N - k;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+          const float2 a = staged_row(S, kk, r0 + t), b = staged_row(S, M + kk, r0 + t);
+          if (k == 0) v[t][q] = make_float2(a.x, b.x);
+          else if (k < M) v[t][q] = make_float2(a.x - b.y, a.y + b.x);
+          else v[t][q] = make_float2(a.x + b.y, b.x - a.y);
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < NT; ++t) v[t][q] = make_float2(0.f, 0.f);
+      }
+    }
+  };
+  int rp = blockIdx.x;
+  if (rp >= NRP) return;  // uniform for the whole CTA
+  stage_plane_pair<THREADS>(S0, P + (size_t)rp * M, P + pl4 + (size_t)rp * M, M, true);
+  stage_plane_pair<THREADS>(S1, P + 2 * pl4 + (size_t)rp * M, P + 3 * pl4 + (size_t)rp * M, M, true);
+  for (; rp < NRP; rp += gridDim.x) {
+    const int y0 = 2 * rp;
+    const int nx = rp + gridDim.x;
+    const bool more = nx < NRP;
+    cpx<T> v[NT][E];
+    // The four transforms of the row pair run through one copy of the
+    // transform code (a loop that is not unrolled): unrolled, the compiler
+    // interleaves them and runs out of registers.  The forward transform is
+    // the inverse one of the conjugate, conjugated (bit-identical).
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+      if (f < 3) {
+        // pending copy groups: f = 0: pairs 1, 2; f = 1: pairs 2, 3; f = 2: pair 3
+        if (f == 2) cp_async_wait<0>();
+        else cp_async_wait<1>();
+        __syncthreads();  // the staged pair is visible; the previous users of sm are done
+        load_z(f == 1 ? S1 : S0, v);
+        __syncthreads();  // every read of the staging buffer is done
+        if (f == 0) {
+          stage_plane_pair<THREADS>(S0, P + 4 * pl4 + (size_t)rp * M, P + 5 * pl4 + (size_t)rp * M, M, true);
+        } else if (f == 2) {
+          stage_plane_pair<THREADS>(S0, P + (size_t)nx * M, P + pl4 + (size_t)nx * M, M, more);
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < NT; ++t)
+#pragma unroll
+          for (int q = 0; q < E; ++q) v[t][q].y = -v[t][q].y;
+      }
+      F::template run<+1>(v, lane, sm, tw);
+      if (f == 0) {
+        if constexpr (CFL) {
+          double m = 0.0;
+#pragma unroll
+          for (int t = 0; t < NT; ++t)
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+              const double rx = (double)v[t][q].x, ry = (double)v[t][q].y;
+              m = fmax(m, rx * rx + ry * ry);
+            }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+          if ((threadIdx.x & 31) == 0) atomicMax(cfl_enc, enc_ordered(m));
+        }
+        // each thread reads back only the positions it wrote: no barrier needed
+#pragma unroll
+        for (int t = 0; t < NT; ++t)
+#pragma unroll
+          for (int q = 0; q < E; ++q) hold[t * N + lane + q * TPF] = v[t][q];
+      } else if (f == 1) {
+#pragma unroll
+        for (int t = 0; t < NT; ++t)
+#pragma unroll
+          for (int q = 0; q < E; ++q) {
+            const cpx<T> a = hold[t * N + lane + q * TPF];
+            P1[t * N + lane + q * TPF] = (a.x * v[t][q].y - a.y * v[t][q].x) * inv_n4;
+          }
+      } else if (f == 2) {
+#pragma unroll
+        for (int t = 0; t < NT; ++t)
+#pragma unroll
+          for (int q = 0; q < E; ++q) {
+            const cpx<T> a = hold[t * N + lane + q * TPF];
+            v[t][q] = mkc<T>(P1[t * N + lane + q * TPF], (a.x * v[t][q].y - a.y * v[t][q].x) * inv_n4);
+          }
+      } else {
+#pragma unroll
+        for (int t = 0; t < NT; ++t)
+#pragma unroll
+          for (int q = 0; q < E; ++q) v[t][q].y = -v[t][q].y;
+      }
+    }
+    F::to_smem(v, lane, sm);
+    __syncthreads();  // also ends every read of p1 in S1
+    stage_plane_pair<THREADS>(S1, P + 2 * pl4 + (size_t)nx * M, P + 3 * pl4 + (size_t)nx * M, M, more);
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int k = lane + q * TPF;
+      if (k < kxo) {
+        cpx<T> o1[NT], o2[NT];
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+          const cpx<T> w = F::from_smem(t, k, sm);
+          const cpx<T> u = F::from_smem(t, (N - k) & (N - 1), sm);
+          o1[t] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
+          o2[t] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+        }
+        const size_t off = mix_idx<N, 2>(k, y0 + r0, gd.nh);
+        if constexpr (NT == 2) {
+          store_rows<T, 2>(pb, off, o1);
+          store_rows<T, 2>(pb + oplane, off, o2);
+        } else {
+          pb[off] = o1[0];
+          pb[oplane + off] = o2[0];
+        }
+      }
+    }
+  }
+  cp_async_wait<0>();  // no copy outlives the CTA
+}
+
+// --------------------------------------------------------------------------
 // pass C: forward y-FFT of both brackets + RK substep update
 // (Rot2D3C.para.f90:578-599).  c1in/c2in may alias c1out/c2out, and in the
 // last substep c1out/c2out are ps/vz themselves: every element is read and
 // written by the same thread.
 // --------------------------------------------------------------------------
+// The inputs of one element's update, loaded ahead of the arithmetic so that
+// a batch of elements can have all its loads in flight before its first
+// store (the output planes may alias the inputs, which keeps the compiler
+// from reordering loads and stores itself).
 template <typename T>
-__device__ __forceinline__ void rk_update(const cpx<T> c5, const cpx<T> c6, size_t idx, int kyi, int k2,
-                                          const cpx<T>* c1in, const cpx<T>* c2in, const cpx<T>* ps,
-                                          const cpx<T>* vz, const cpx<T>* __restrict__ fp,
-                                          const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out,
-                                          const StepCoef& sc, T tmp1, int kmaxi) {
-  cpx<T> n1 = czero<T>(), n2 = czero<T>();
-  if (k2 <= kmaxi && k2 >= 1) {  // ka2 <= kmax .and. ka2 > tiny (:580)
-    const T nu = (T)sc.nu, hnu = (T)sc.hnu, nuv = (T)sc.nuv, hnuv = (T)sc.hnuv, w2 = (T)sc.w2;
-    const cpx<T> a1 = c1in[idx], a2 = c2in[idx];
-    const T kyf = (T)kyi, ka2 = (T)k2;
-    const cpx<T> C3 = mkc<T>(-kyf * a1.y, kyf * a1.x);  // derivk2(C1,C3,2)
-    const cpx<T> C4 = mkc<T>(-kyf * a2.y, kyf * a2.x);  // derivk2(C2,C4,2)
-    const T tmp2 = (T)1 / ka2;
-    const T tmp3 = (T)1 + (nu * powi(ka2, sc.nn) + hnu * powi(tmp2, sc.mm)) * tmp1;
-    const cpx<T> p0 = ps[idx], f0 = fp[idx];
-    const T u1x = p0.x + ((-c5.x + w2 * C4.x) * tmp2 + f0.x) * tmp1;
-    const T u1y = p0.y + ((-c5.y + w2 * C4.y) * tmp2 + f0.y) * tmp1;
-    n1 = mkc<T>(u1x / tmp3, u1y / tmp3);
-    const T tmp3v = (T)1 + (nuv * powi(ka2, sc.nnv) + hnuv * powi(tmp2, sc.mmv)) * tmp1;
-    const cpx<T> v0 = vz[idx], g0 = fz[idx];
-    const T u2x = v0.x + (c6.x + w2 * C3.x + g0.x) * tmp1;
-    const T u2y = v0.y + (c6.y + w2 * C3.y + g0.y) * tmp1;
-    n2 = mkc<T>(u2x / tmp3v, u2y / tmp3v);
-  }
-  c1out[idx] = n1;
-  c2out[idx] = n2;
+struct RkIn {
+  cpx<T> a1, a2, p0, f0, v0, g0;
+};
+
+template <typename T>
+__device__ __forceinline__ void rk_load(RkIn<T>& r, size_t idx, const cpx<T>* c1in, const cpx<T>* c2in,
+                                        const cpx<T>* ps, const cpx<T>* vz, const cpx<T>* __restrict__ fp,
+                                        const cpx<T>* __restrict__ fz) {
+  r.a1 = c1in[idx];
+  r.a2 = c2in[idx];
+  r.p0 = ps[idx];
+  r.f0 = fp[idx];
+  r.v0 = vz[idx];
+  r.g0 = fz[idx];
+}
+
+// New C1, C2 of one element (Rot2D3C.para.f90:580-599); zero outside the
+// retained disc and at k = 0.
+template <typename T>
+__device__ __forceinline__ void rk_apply(const RkIn<T>& r, const cpx<T> c5, const cpx<T> c6, int kyi, int k2,
+                                         const StepCoef& sc, T tmp1, cpx<T>& n1, cpx<T>& n2) {
+  const T nu = (T)sc.nu, hnu = (T)sc.hnu, nuv = (T)sc.nuv, hnuv = (T)sc.hnuv, w2 = (T)sc.w2;
+  const T kyf = (T)kyi, ka2 = (T)k2;
+  const cpx<T> C3 = mkc<T>(-kyf * r.a1.y, kyf * r.a1.x);  // derivk2(C1,C3,2)
+  const cpx<T> C4 = mkc<T>(-kyf * r.a2.y, kyf * r.a2.x);  // derivk2(C2,C4,2)
+  const T tmp2 = (T)1 / ka2;
+  const T tmp3 = (T)1 + (nu * powi(ka2, sc.nn) + hnu * powi(tmp2, sc.mm)) * tmp1;
+  const T u1x = r.p0.x + ((-c5.x + w2 * C4.x) * tmp2 + r.f0.x) * tmp1;
+  const T u1y = r.p0.y + ((-c5.y + w2 * C4.y) * tmp2 + r.f0.y) * tmp1;
+  n1 = mkc<T>(u1x / tmp3, u1y / tmp3);
+  const T tmp3v = (T)1 + (nuv * powi(ka2, sc.nnv) + hnuv * powi(tmp2, sc.mmv)) * tmp1;
+  const T u2x = r.v0.x + (c6.x + w2 * C3.x + r.g0.x) * tmp1;
+  const T u2y = r.v0.y + (c6.y + w2 * C3.y + r.g0.y) * tmp1;
+  n2 = mkc<T>(u2x / tmp3v, u2y / tmp3v);
+}
+
+// L2 prefetch (cp.async.bulk.prefetch, no completion to wait for) of the
+// retained rows |ky| <= L of ncol adjacent spectral columns starting at p:
+// rows [0, L] of the first column, then each run [N - L, N + L] across a
+// column boundary, then rows [N - L, N) of the last column.
+// The range is widened to 16-byte boundaries (the instruction's alignment
+// rule); every caller's range lies inside columns that start and end on
+// 16-byte boundaries, so the widened range stays inside the same allocation.
+template <typename T>
+__device__ __forceinline__ void prefetch_l2(const T* p, size_t count) {
+  const unsigned long long a0 = reinterpret_cast<unsigned long long>(p) & ~15ull;
+  const unsigned long long a1 = (reinterpret_cast<unsigned long long>(p + count) + 15ull) & ~15ull;
+  if (a1 > a0)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a0), "r"((unsigned)(a1 - a0)) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ void prefetch_columns_l2(const cpx<T>* p, int ncol, int N, int L) {
+  prefetch_l2(p, (size_t)L + 1);
+  for (int c = 1; c < ncol; ++c) prefetch_l2(p + (size_t)c * N - L, (size_t)2 * L + 1);
+  prefetch_l2(p + (size_t)ncol * N - L, (size_t)L);
 }
 
 template <typename T, int N>
@@ -580,20 +846,32 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   fz += rs;
   c1out += rs;
   c2out += rs;
-  const StepCoef sc = scs[blockIdx.y];
-  const double* dtp = scal + blockIdx.y * kScalStride;
   using C = Cfg<T, N, NT>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
-  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  const int g = threadIdx.x / C::TPF, lane0 = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
   cpx<T>* hold = sm + NT * F::SMEM_ELEMS;  // transformed [psi,-k^2 psi] columns (HOLD)
   const int kx0 = (blockIdx.x * C::G + g) * NT;
   const size_t oplane = (size_t)gd.nh * N;
+  // The RK update at the end reads six spectral planes (eight with the
+  // closure tendencies) on this group's columns; they are prefetched into L2
+  // now, while the transforms run, so that those reads do not wait for DRAM.
+  if (lane0 < 8) {
+    const int lane = lane0;
+    const cpx<T>* src = lane == 0 ? c1in : lane == 1 ? c2in : lane == 2 ? ps : lane == 3 ? vz
+                      : lane == 4 ? fp : lane == 5 ? fz : lane == 6 ? tau5 : tau6;
+    const int ncol = min(NT, gd.M - kx0);
+    if (src && ncol > 0) prefetch_columns_l2<T>(src + (size_t)kx0 * N, ncol, N, gd.L);
+  }
   cpx<T> v[NT][C::E];
   cpx<T> c5r[HOLD ? 1 : NT][C::E];
 #pragma unroll 1
   for (int pl = 0; pl < 2; ++pl) {
+    // the loop-invariant addresses of the transform are recomputed per
+    // iteration from an opaque copy of the lane index instead of being
+    // hoisted out of the loop and held in registers across it
+    const int lane = opaque(lane0);
     const cpx<T>* src = pb + pl * oplane;
     if constexpr (NT == 2) {
       // lane pair (2p, 2p+1): the even lane loads column kx0's rows (2p, 2p+1),
@@ -632,30 +910,86 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         }
     }
   }
-  // v holds the transformed [psi, vz] columns; c5 is read back per element
-  // by the thread that stored it (no barrier needed)
-  const T tmp1 = (T)(*dtp / (double)o);  // :581
+  const int lane = lane0;
+  // v holds the transformed [psi, vz] columns (c6).  The coefficients are
+  // read only now, not held in registers across the transforms.
+  const StepCoef sc = scs[blockIdx.y];
+  const T tmp1 = (T)(scal[blockIdx.y * kScalStride] / (double)o);  // :581
+  if constexpr (HOLD) {
+    // c6 joins c5 in shared memory (the transform buffer is free after the
+    // last transform; each thread reads back only what it wrote), and the
+    // update runs over this thread's elements in batches of RB: all loads of
+    // a batch, then its arithmetic and stores.
+    cpx<T>* c6s = sm;
 #pragma unroll
-  for (int t = 0; t < NT; ++t) {
-    const int col = kx0 + t;
-    if (col >= gd.M) continue;
+    for (int t = 0; t < NT; ++t)
 #pragma unroll
-    for (int q = 0; q < C::E; ++q) {
-      const int j = lane + q * C::TPF;
-      const int ky = ky_of(j, N);
-      if (ky > gd.L || -ky > gd.L) continue;
-      cpx<T> c5;
-      if constexpr (HOLD) c5 = hold[t * N + j];
-      else c5 = c5r[t][q];
-      cpx<T> c6 = v[t][q];
-      const size_t idx = (size_t)col * N + j;
-      if (tau5) {  // learned subgrid tendencies of the two brackets
-        const cpx<T> a = tau5[idx], b = tau6[idx];
-        c5 = mkc<T>(c5.x + a.x, c5.y + a.y);
-        c6 = mkc<T>(c6.x + b.x, c6.y + b.y);
+      for (int q = 0; q < C::E; ++q) c6s[t * N + lane + q * C::TPF] = v[t][q];
+    constexpr int NE = NT * C::E, RB = 2;
+    static_assert(NE % RB == 0, "whole batches");
+#pragma unroll 1
+    for (int e0 = 0; e0 < NE; e0 += RB) {
+      RkIn<T> in[RB];
+      cpx<T> ta[RB], tb[RB];
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const int t = (e0 + b) / C::E, q = (e0 + b) % C::E;
+        const int col = kx0 + t, j = lane + q * C::TPF, ky = ky_of(j, N), k2 = col * col + ky * ky;
+        if (col < gd.M && k2 <= gd.kmaxi && k2 >= 1) {
+          const size_t idx = (size_t)col * N + j;
+          rk_load<T>(in[b], idx, c1in, c2in, ps, vz, fp, fz);
+          if (tau5) {
+            ta[b] = tau5[idx];
+            tb[b] = tau6[idx];
+          }
+        }
       }
-      rk_update<T>(c5, c6, idx, ky, col * col + ky * ky, c1in, c2in, ps, vz, fp, fz, c1out, c2out, sc, tmp1,
-                   gd.kmaxi);
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const int t = (e0 + b) / C::E, q = (e0 + b) % C::E;
+        const int col = kx0 + t, j = lane + q * C::TPF, ky = ky_of(j, N), k2 = col * col + ky * ky;
+        if (col >= gd.M || ky > gd.L || -ky > gd.L) continue;
+        cpx<T> n1 = czero<T>(), n2 = czero<T>();
+        if (k2 <= gd.kmaxi && k2 >= 1) {  // ka2 <= kmax .and. ka2 > tiny (:580)
+          cpx<T> c5 = hold[t * N + j], c6 = c6s[t * N + j];
+          if (tau5) {  // learned subgrid tendencies of the two brackets
+            c5 = mkc<T>(c5.x + ta[b].x, c5.y + ta[b].y);
+            c6 = mkc<T>(c6.x + tb[b].x, c6.y + tb[b].y);
+          }
+          rk_apply<T>(in[b], c5, c6, ky, k2, sc, tmp1, n1, n2);
+        }
+        const size_t idx = (size_t)col * N + j;
+        c1out[idx] = n1;
+        c2out[idx] = n2;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int col = kx0 + t;
+      if (col >= gd.M) continue;
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) {
+        const int j = lane + q * C::TPF;
+        const int ky = ky_of(j, N);
+        if (ky > gd.L || -ky > gd.L) continue;
+        const int k2 = col * col + ky * ky;
+        cpx<T> n1 = czero<T>(), n2 = czero<T>();
+        const size_t idx = (size_t)col * N + j;
+        if (k2 <= gd.kmaxi && k2 >= 1) {
+          cpx<T> c5 = c5r[t][q], c6 = v[t][q];
+          if (tau5) {
+            const cpx<T> a = tau5[idx], b = tau6[idx];
+            c5 = mkc<T>(c5.x + a.x, c5.y + a.y);
+            c6 = mkc<T>(c6.x + b.x, c6.y + b.y);
+          }
+          RkIn<T> in;
+          rk_load<T>(in, idx, c1in, c2in, ps, vz, fp, fz);
+          rk_apply<T>(in, c5, c6, ky, k2, sc, tmp1, n1, n2);
+        }
+        c1out[idx] = n1;
+        c2out[idx] = n2;
+      }
     }
   }
 }

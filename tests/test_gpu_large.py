@@ -1,0 +1,59 @@
+"""The FP32 grids that run the pipelined, persistent pass B (n = 2048, 4096)
+and the radix-16 transforms: steps against the FP64 path on the same inputs
+(the FP64 path matches the oracle to 1e-12 at the sizes the oracle runs
+quickly), the CFL time step of the fused maximum, and batched runs against
+single runs (bit-exact: every row pair is computed the same way whatever CTA
+carries it)."""
+import numpy as np
+import pytest
+
+from tests._helpers import params, random_forcing, random_state, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(n, seed):
+    _, cp = params(n, omega=2.0, nu=1e-5, nuv=1e-5, hnu=0.1, hnuv=0.1, iflow=0)
+    g, ps, vz = random_state(n, seed, kmax_shell=100.0, slope=-3.0, amp=float(n) ** 2)
+    fp, fz = random_forcing(g, seed + 1, 20.0, 22.0)
+    return cp, ps, vz, fp, fz
+
+
+def _advance(gpu, prec, cp, ps, vz, fp, fz, nsteps, mode, val):
+    c = gpu.Context(cp, prec)
+    c.set_state(ps, vz)
+    c.set_forcing(fp, fz)
+    c.set_time(0.0)
+    t, dt = c.advance(nsteps, mode, val)
+    a, b = c.get_state()
+    c.destroy()
+    return a, b, t, dt
+
+
+@pytest.mark.parametrize("n", [2048, 4096])
+def test_fp32_cfl_steps_match_fp64(gpu, n):
+    cp, ps, vz, fp, fz = _case(n, 7)
+    a32, b32, t32, dt32 = _advance(gpu, 1, cp, ps, vz, fp, fz, 3, gpu.DT_CFL, 0.5)
+    a64, b64, t64, dt64 = _advance(gpu, 0, cp, ps, vz, fp, fz, 3, gpu.DT_CFL, 0.5)
+    assert abs(dt32 - dt64) <= 1e-5 * dt64
+    assert abs(t32 - t64) <= 1e-5 * t64
+    assert rel_l2(a32, a64) < 1e-5
+    assert rel_l2(b32, b64) < 1e-5
+
+
+@pytest.mark.parametrize("n", [2048, 4096])
+def test_fp32_batched_equals_single(gpu, n):
+    runs = [_case(n, 30 + 2 * i) for i in range(2)]
+    ens = gpu.Ensemble([(n, [r[0] for r in runs])], 1)
+    for i, (cp, ps, vz, fp, fz) in enumerate(runs):
+        ens.set_state(i, ps, vz)
+        ens.set_forcing(i, fp, fz)
+        ens.set_time(i, 0.0)
+    times = ens.advance(2, gpu.DT_CFL, 0.5)
+    for i, (cp, ps, vz, fp, fz) in enumerate(runs):
+        a, b, t, _ = _advance(gpu, 1, cp, ps, vz, fp, fz, 2, gpu.DT_CFL, 0.5)
+        ea, eb = ens.get_state(i)
+        np.testing.assert_array_equal(ea, a)
+        np.testing.assert_array_equal(eb, b)
+        assert times[i] == t
+    ens.destroy()
