@@ -14,6 +14,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -63,190 +64,238 @@ __device__ __forceinline__ float gelu_d(float x) {
 }
 
 // ---------------------------------------------------------------------------
-// out[p][co] = sum_k in_col[p][k] w[k][co] (+ bias), periodic 3x3 stencil.
-// in: [B][H][W][CIN] bf16; w: [9*CIN][COUT] bf16; y: [B][H][W][COUT] f32
-// (pre-activation, may be null); a: [B][H][W][COUT] bf16 = act(y) (may be
-// null); act: 0 identity, 1 GELU.  Requires H % TH == 0, W % TW == 0.
+// Shared-memory tiles hold rows of C bf16 values (a pixel's channels, or a
+// weight row's output channels) as C/8 chunks of 16 bytes; chunk c of row r
+// is stored at chunk position c ^ swz(r) so that the 8 rows an ldmatrix
+// reads (8 consecutive pixels, or 8 consecutive weight rows) fall in 8
+// different bank groups.
 // ---------------------------------------------------------------------------
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(kThreads)
-k_conv(const bf16* __restrict__ in, const bf16* __restrict__ w, const float* __restrict__ bias, int H, int W,
-       float* __restrict__ y, bf16* __restrict__ a, int act, int cout_store) {
-  constexpr int NTN = COUT / 8;  // n-tiles
-  __shared__ __align__(16) bf16 s_in[(TH + 2) * (TW + 2) * CIN];
-  __shared__ __align__(16) bf16 s_w[9 * CIN * COUT];
-  const int tiles_x = W / TW, tiles_y = H / TH;
-  const int t = blockIdx.x;
-  const int b = t / (tiles_x * tiles_y);
-  const int ty0 = ((t / tiles_x) % tiles_y) * TH, tx0 = (t % tiles_x) * TW;
-  // stage the weights and the halo tile (periodic wrap)
-  for (int i = threadIdx.x; i < 9 * CIN * COUT / 8; i += kThreads)
-    reinterpret_cast<uint4*>(s_w)[i] = reinterpret_cast<const uint4*>(w)[i];
-  constexpr int VPP = CIN / 8;  // 16-byte vectors per pixel
+template <int C>
+__device__ __forceinline__ int swz(int r) {
+  constexpr int C8 = C / 8;
+  static_assert(C8 == 2 || C8 == 4, "16 or 32 channels");
+  return (r / (8 / C8)) % C8;
+}
+template <int C>
+__device__ __forceinline__ int tile_off(int r, int chunk) {  // bf16 offset of (row, chunk)
+  return r * C + ((chunk ^ swz<C>(r)) << 3);
+}
+
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x4_t(unsigned (&r)[4], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2_t(unsigned (&r)[2], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(r[0]), "=r"(r[1])
+               : "r"(a));
+}
+
+// Halo tile (TH+2) x (TW+2) pixels of CIN channels around tile (b, ty0, tx0),
+// periodic wrap, into the swizzled layout.
+template <int CIN>
+__device__ __forceinline__ void stage_halo(bf16* s_in, const bf16* __restrict__ in, int b, int ty0, int tx0, int H,
+                                           int W) {
+  constexpr int VPP = CIN / 8;
   for (int i = threadIdx.x; i < (TH + 2) * (TW + 2) * VPP; i += kThreads) {
-    const int v = i % VPP, px = (i / VPP) % (TW + 2), py = (i / VPP) / (TW + 2);
+    const int v = i % VPP, q = i / VPP, px = q % (TW + 2), py = q / (TW + 2);
     const int gy = (ty0 + py - 1 + H) % H, gx = (tx0 + px - 1 + W) % W;
-    reinterpret_cast<uint4*>(s_in)[i] =
+    *reinterpret_cast<uint4*>(s_in + tile_off<CIN>(q, v)) =
         reinterpret_cast<const uint4*>(in + (((size_t)b * H + gy) * W + gx) * CIN)[v];
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gid = lane >> 2, tig = lane & 3;
-  float acc[NTN][4];
-#pragma unroll
-  for (int n = 0; n < NTN; ++n)
-#pragma unroll
-    for (int r = 0; r < 4; ++r) acc[n][r] = 0.f;
-  // warp handles tile row `warp`, pixels x = 0..15 of the tile
-#pragma unroll
-  for (int tap = 0; tap < 9; ++tap) {
-    const int dy = tap / 3, dx = tap % 3;
-#pragma unroll
-    for (int c0 = 0; c0 < CIN; c0 += 16) {
-      // A (16 x 16): rows = pixels gid and gid+8, cols = channels c0 + tig*2 (+1, +8, +9)
-      const bf16* r0 = s_in + ((warp + dy) * (TW + 2) + (gid + dx)) * CIN + c0 + tig * 2;
-      const bf16* r1 = s_in + ((warp + dy) * (TW + 2) + (gid + 8 + dx)) * CIN + c0 + tig * 2;
-      unsigned af[4];
-      af[0] = *reinterpret_cast<const unsigned*>(r0);
-      af[1] = *reinterpret_cast<const unsigned*>(r1);
-      af[2] = *reinterpret_cast<const unsigned*>(r0 + 8);
-      af[3] = *reinterpret_cast<const unsigned*>(r1 + 8);
-      const int k0 = tap * CIN + c0;
-#pragma unroll
-      for (int n = 0; n < NTN; ++n) {
-        // B (16 x 8): rows k = k0 + tig*2 (+1, +8, +9), col co = n*8 + gid
-        const int co = n * 8 + gid;
-        unsigned bfr[2];
-        bfr[0] = pack_bf16(s_w[(k0 + tig * 2) * COUT + co], s_w[(k0 + tig * 2 + 1) * COUT + co]);
-        bfr[1] = pack_bf16(s_w[(k0 + tig * 2 + 8) * COUT + co], s_w[(k0 + tig * 2 + 9) * COUT + co]);
-        mma_bf16(acc[n], af, bfr);
-      }
-    }
-  }
-  // D: rows gid, gid+8 (pixels), cols n*8 + tig*2 (+1)
-  const int gy = ty0 + warp;
-#pragma unroll
-  for (int half = 0; half < 2; ++half) {
-    const int gx = tx0 + gid + half * 8;
-    const size_t pix = ((size_t)b * H + gy) * W + gx;
-#pragma unroll
-    for (int n = 0; n < NTN; ++n)
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        const int co = n * 8 + tig * 2 + e;
-        if (co >= cout_store) continue;
-        float v = acc[n][half * 2 + e] + (bias ? bias[co] : 0.f);
-        if (y) y[pix * cout_store + co] = v;
-        if (a) a[pix * COUT + co] = __float2bfloat16_rn(act ? gelu(v) : v);
-      }
   }
 }
 
 // ---------------------------------------------------------------------------
-// dW[k][co] partials: CTA c accumulates over pixel tiles c, c + grid, ...
-// in: [B][H][W][CIN] bf16, dy: [B][H][W][COUT] bf16; part: [grid][9*CIN*COUT]
+// out[p][co] = sum_k in_col[p][k] w[k][co] (+ bias), periodic 3x3 stencil.
+// in: [B][H][W][CIN] bf16; w: [9*CIN][COUT] bf16; y: [B][H][W][cout_store] f32
+// (pre-activation, may be null); a: [B][H][W][COUT] bf16 = act(y) (may be
+// null); act: 0 identity, 1 GELU.  Requires H % TH == 0, W % TW == 0.
+// Persistent CTAs: the weights are staged once, then the CTA loops over
+// 8 x 16 pixel tiles; warp w computes tile row w (16 pixels x COUT).
+// Fragments come from ldmatrix: A (pixels x k) directly, B (k x co) through
+// the transposing form.
+// ---------------------------------------------------------------------------
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kThreads)
+k_conv(const bf16* __restrict__ in, const bf16* __restrict__ w, const float* __restrict__ bias, int H, int W,
+       int ntiles, float* __restrict__ y, bf16* __restrict__ a, int act, int cout_store) {
+  constexpr int NTN = COUT / 8;  // n-tiles
+  static_assert(NTN % 2 == 0, "n-tiles in pairs");
+  __shared__ __align__(128) bf16 s_in[(TH + 2) * (TW + 2) * CIN];
+  __shared__ __align__(128) bf16 s_w[9 * CIN * COUT];
+  for (int i = threadIdx.x; i < 9 * CIN * COUT / 8; i += kThreads) {
+    const int r = i / (COUT / 8), c = i % (COUT / 8);
+    *reinterpret_cast<uint4*>(s_w + tile_off<COUT>(r, c)) = reinterpret_cast<const uint4*>(w)[i];
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int lj = lane >> 3, lr = lane & 7;  // ldmatrix: matrix and row this lane addresses
+  const int tiles_x = W / TW, tiles_y = H / TH;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int b = t / (tiles_x * tiles_y);
+    const int ty0 = ((t / tiles_x) % tiles_y) * TH, tx0 = (t % tiles_x) * TW;
+    __syncthreads();  // weights staged / previous tile's reads done
+    stage_halo<CIN>(s_in, in, b, ty0, tx0, H, W);
+    __syncthreads();
+    float acc[NTN][4];
+#pragma unroll
+    for (int n = 0; n < NTN; ++n)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[n][r] = 0.f;
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+      const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+      for (int c0 = 0; c0 < CIN; c0 += 16) {
+        // A: matrices (px 0-7 | 8-15) x (k c0..c0+7 | c0+8..c0+15)
+        unsigned af[4];
+        {
+          const int q = (warp + dy) * (TW + 2) + lr + 8 * (lj & 1) + dx;
+          ldsm_x4(af, s_in + tile_off<CIN>(q, (c0 >> 3) + (lj >> 1)));
+        }
+        const int k0 = tap * CIN + c0;
+#pragma unroll
+        for (int n = 0; n < NTN; n += 2) {
+          // B: matrices (k0..k0+7 | k0+8..) x (co n*8.. | (n+1)*8..), transposed
+          unsigned bq[4];
+          ldsm_x4_t(bq, s_w + tile_off<COUT>(k0 + lr + 8 * (lj & 1), n + (lj >> 1)));
+          const unsigned b0[2] = {bq[0], bq[1]}, b1[2] = {bq[2], bq[3]};
+          mma_bf16(acc[n], af, b0);
+          mma_bf16(acc[n + 1], af, b1);
+        }
+      }
+    }
+    // D: rows gid, gid+8 (pixels), cols n*8 + tig*2 (+1)
+    const int gy = ty0 + warp;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int gx = tx0 + gid + half * 8;
+      const size_t pix = ((size_t)b * H + gy) * W + gx;
+#pragma unroll
+      for (int n = 0; n < NTN; ++n) {
+        const int co = n * 8 + tig * 2;
+        if (co >= cout_store) continue;
+        const float v0 = acc[n][half * 2] + (bias ? bias[co] : 0.f);
+        const float v1 = acc[n][half * 2 + 1] + (bias ? bias[co + 1] : 0.f);
+        if (y) *reinterpret_cast<float2*>(y + pix * cout_store + co) = make_float2(v0, v1);
+        if (a)
+          *reinterpret_cast<__nv_bfloat162*>(a + pix * COUT + co) =
+              __halves2bfloat162(__float2bfloat16_rn(act ? gelu(v0) : v0), __float2bfloat16_rn(act ? gelu(v1) : v1));
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dW[k][co] and db[co] partials: CTA c accumulates over pixel tiles c,
+// c + grid, ...  in: [B][H][W][CIN] bf16, dy: [B][H][W][COUT] bf16;
+// part: [grid][9*CIN*COUT + COUT] (weights, then bias).  The GEMM is
+// dW = in_col^T dY over the tile's 128 pixels (8 k-steps of one tile row);
+// warp w owns the m-tiles (16 rows of k) w, w+8, w+16 and all n-tiles.
+// Both fragments come from the transposing ldmatrix.
 // ---------------------------------------------------------------------------
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(kThreads)
 k_conv_wgrad(const bf16* __restrict__ in, const bf16* __restrict__ dy, int H, int W, int ntiles,
              float* __restrict__ part) {
-  constexpr int K = 9 * CIN, MT = K / 16, NTN = COUT / 8, PAIRS = MT * NTN;
-  constexpr int PPW = (PAIRS + 7) / 8;  // (m,n) tile pairs per warp
-  __shared__ __align__(16) bf16 s_in[(TH + 2) * (TW + 2) * CIN];
-  __shared__ __align__(16) bf16 s_dy[TH * TW * COUT];
+  constexpr int K = 9 * CIN, MT = K / 16, NTN = COUT / 8;
+  constexpr int MPW = (MT + 7) / 8;  // m-tiles per warp (at most)
+  static_assert(NTN % 2 == 0, "n-tiles in pairs");
+  __shared__ __align__(128) bf16 s_in[(TH + 2) * (TW + 2) * CIN];
+  __shared__ __align__(128) bf16 s_dy[TH * TW * COUT];
+  __shared__ float s_b[kThreads];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gid = lane >> 2, tig = lane & 3;
-  float acc[PPW][4];
+  const int lj = lane >> 3, lr = lane & 7;
+  float acc[MPW][NTN][4];
 #pragma unroll
-  for (int i = 0; i < PPW; ++i)
+  for (int i = 0; i < MPW; ++i)
 #pragma unroll
-    for (int r = 0; r < 4; ++r) acc[i][r] = 0.f;
+    for (int n = 0; n < NTN; ++n)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][n][r] = 0.f;
+  float bsum = 0.f;  // bias partial of channel threadIdx.x % COUT
   const int tiles_x = W / TW, tiles_y = H / TH;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int b = t / (tiles_x * tiles_y);
     const int ty0 = ((t / tiles_x) % tiles_y) * TH, tx0 = (t % tiles_x) * TW;
     __syncthreads();
-    constexpr int VPP = CIN / 8;
-    for (int i = threadIdx.x; i < (TH + 2) * (TW + 2) * VPP; i += kThreads) {
-      const int v = i % VPP, px = (i / VPP) % (TW + 2), py = (i / VPP) / (TW + 2);
-      const int gy = (ty0 + py - 1 + H) % H, gx = (tx0 + px - 1 + W) % W;
-      reinterpret_cast<uint4*>(s_in)[i] =
-          reinterpret_cast<const uint4*>(in + (((size_t)b * H + gy) * W + gx) * CIN)[v];
-    }
+    stage_halo<CIN>(s_in, in, b, ty0, tx0, H, W);
     constexpr int VPO = COUT / 8;
     for (int i = threadIdx.x; i < TH * TW * VPO; i += kThreads) {
-      const int v = i % VPO, px = (i / VPO) % TW, py = (i / VPO) / TW;
-      reinterpret_cast<uint4*>(s_dy)[i] =
+      const int v = i % VPO, p = i / VPO, px = p % TW, py = p / TW;
+      *reinterpret_cast<uint4*>(s_dy + tile_off<COUT>(p, v)) =
           reinterpret_cast<const uint4*>(dy + (((size_t)b * H + ty0 + py) * W + tx0 + px) * COUT)[v];
     }
     __syncthreads();
-    // reduction over the 128 pixels of the tile in 8 k-steps of 16 (one tile row each)
+    {  // bias: fixed pixel order per thread
+      const int co = threadIdx.x % COUT;
+      for (int p = threadIdx.x / COUT; p < TH * TW; p += kThreads / COUT)
+        bsum += __bfloat162float(s_dy[tile_off<COUT>(p, co >> 3) + (co & 7)]);
+    }
 #pragma unroll 1
     for (int ks = 0; ks < TH; ++ks) {
+      // B fragments of this k-step (pixels ks*TW .. +15) for every n-tile
+      unsigned bq[NTN / 2][4];
 #pragma unroll
-      for (int i = 0; i < PPW; ++i) {
-        const int pair = warp * PPW + i;
-        if (pair >= PAIRS) break;
-        const int mt = pair / NTN, nt = pair % NTN;
-        // A (16 x 16) = in_col^T: rows m = k index mt*16 + gid (+8), cols = pixels tig*2 (+1, +8, +9)
+      for (int n = 0; n < NTN; n += 2)
+        ldsm_x4_t(bq[n / 2], s_dy + tile_off<COUT>(ks * TW + lr + 8 * (lj & 1), n + (lj >> 1)));
+#pragma unroll
+      for (int i = 0; i < MPW; ++i) {
+        const int mt = warp + 8 * i;
+        if (mt >= MT) break;
+        const int tap = (mt * 16) / CIN, ci0 = (mt * 16) % CIN, dyy = tap / 3, dxx = tap % 3;
+        // A = in_col^T: matrices (px 0-7 | 8-15) x (ch ci0.. | ci0+8..), transposed
         unsigned af[4];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {      // rows gid, gid + 8
-#pragma unroll
-          for (int c = 0; c < 2; ++c) {    // pixel columns tig*2 + c*8
-            const int k = mt * 16 + gid + h * 8;
-            const int tap = k / CIN, ci = k % CIN, dyy = tap / 3, dxx = tap % 3;
-            const int px = tig * 2 + c * 8;
-            const bf16 v0 = s_in[((ks + dyy) * (TW + 2) + px + dxx) * CIN + ci];
-            const bf16 v1 = s_in[((ks + dyy) * (TW + 2) + px + 1 + dxx) * CIN + ci];
-            af[h + 2 * c] = pack_bf16(v0, v1);
-          }
+        {
+          const int q = (ks + dyy) * (TW + 2) + lr + 8 * (lj >> 1) + dxx;
+          ldsm_x4_t(af, s_in + tile_off<CIN>(q, (ci0 >> 3) + (lj & 1)));
         }
-        // B (16 x 8) = dY: rows = pixels tig*2 (+1, +8, +9), col = co nt*8 + gid
-        const int co = nt * 8 + gid;
-        unsigned bfr[2];
-        bfr[0] = pack_bf16(s_dy[(ks * TW + tig * 2) * COUT + co], s_dy[(ks * TW + tig * 2 + 1) * COUT + co]);
-        bfr[1] = pack_bf16(s_dy[(ks * TW + tig * 2 + 8) * COUT + co], s_dy[(ks * TW + tig * 2 + 9) * COUT + co]);
-        mma_bf16(acc[i], af, bfr);
+#pragma unroll
+        for (int n = 0; n < NTN; ++n) {
+          const unsigned bf[2] = {bq[n / 2][(n & 1) * 2], bq[n / 2][(n & 1) * 2 + 1]};
+          mma_bf16(acc[i][n], af, bf);
+        }
       }
     }
   }
-  float* out = part + (size_t)blockIdx.x * K * COUT;
+  float* out = part + (size_t)blockIdx.x * (K * COUT + COUT);
+  const int gid = lane >> 2, tig = lane & 3;
 #pragma unroll
-  for (int i = 0; i < PPW; ++i) {
-    const int pair = warp * PPW + i;
-    if (pair >= PAIRS) break;
-    const int mt = pair / NTN, nt = pair % NTN;
+  for (int i = 0; i < MPW; ++i) {
+    const int mt = warp + 8 * i;
+    if (mt >= MT) break;
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
+    for (int n = 0; n < NTN; ++n)
 #pragma unroll
-      for (int e = 0; e < 2; ++e)
-        out[(size_t)(mt * 16 + gid + h * 8) * COUT + nt * 8 + tig * 2 + e] = acc[i][h * 2 + e];
+      for (int h = 0; h < 2; ++h)
+        *reinterpret_cast<float2*>(out + (size_t)(mt * 16 + gid + h * 8) * COUT + n * 8 + tig * 2) =
+            make_float2(acc[i][n][h * 2], acc[i][n][h * 2 + 1]);
+  }
+  s_b[threadIdx.x] = bsum;
+  __syncthreads();
+  if (threadIdx.x < COUT) {
+    float s = 0.f;
+    for (int j = threadIdx.x; j < kThreads; j += COUT) s += s_b[j];
+    out[K * COUT + threadIdx.x] = s;
   }
 }
 
-// grad[i] = sum_c part[c][i] in fixed order; optional bias gradient from dy
+// grad[i] = sum_c part[c][i] in fixed order
 __global__ void k_reduce_parts(const float* __restrict__ part, int nparts, int count, float* __restrict__ grad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   float s = 0.f;
   for (int c = 0; c < nparts; ++c) s += part[(size_t)c * count + i];
   grad[i] = s;
-}
-
-// db[co] = sum_p dy[p][co] (one CTA per channel, fixed-order tree)
-__global__ void k_bias_grad(const bf16* __restrict__ dy, size_t npix, int cstride, float* __restrict__ db) {
-  const int co = blockIdx.x;
-  __shared__ float red[256];
-  float s = 0.f;
-  for (size_t p = threadIdx.x; p < npix; p += blockDim.x) s += __bfloat162float(dy[p * cstride + co]);
-  red[threadIdx.x] = s;
-  __syncthreads();
-  for (int k = 128; k > 0; k >>= 1) {
-    if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) db[co] = red[0];
 }
 
 // dY' = dA * gelu'(y) (bf16), for the hidden layers
@@ -311,13 +360,18 @@ __global__ void k_pack_weights(const float* __restrict__ wm, int cin, int cout, 
   wb[((size_t)(8 - tap) * coutp + co) * cinp + ci] = __float2bfloat16_rn(v);
 }
 
-// padded weight gradient [9][cinp][coutp] -> parameter layout [9][cin][cout]
+// padded weight gradient [9][cinp][coutp] -> parameter layout [9][cin][cout];
+// the padded bias gradient (coutp entries after the weights) -> gb[cout]
 __global__ void k_unpad_wgrad(const float* __restrict__ gp, int cin, int cout, int cinp, int coutp,
-                              float* __restrict__ g) {
+                              float* __restrict__ g, float* __restrict__ gb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 9 * cin * cout) return;
-  const int co = i % cout, ci = (i / cout) % cin, tap = i / (cout * cin);
-  g[i] = gp[((size_t)tap * cinp + ci) * coutp + co];
+  const int nw = 9 * cin * cout;
+  if (i < nw) {
+    const int co = i % cout, ci = (i / cout) % cin, tap = i / (cout * cin);
+    g[i] = gp[((size_t)tap * cinp + ci) * coutp + co];
+  } else if (i < nw + cout) {
+    gb[i - nw] = gp[(size_t)9 * cinp * coutp + (i - nw)];
+  }
 }
 
 // FP32 NHWC [npix][c] -> bf16 NHWC [npix][cp], (x - mean[ch]) / std[ch],
@@ -346,11 +400,24 @@ struct Layer {
   size_t woff, boff;  // offsets in the parameter vector
 };
 
+// Resident CTAs of kernel k on the whole current device (computed once per
+// kernel).
+template <typename K>
+int resident_ctas(K k) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0),
+             "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+  return std::max(1, per_sm) * sms;
+}
+
 template <int CIN, int COUT>
 void conv_launch(const bf16* in, const bf16* w, const float* b, int B, int H, int W, float* y, bf16* a, int act,
                  int cout_store, cudaStream_t st) {
+  static const int ctas = resident_ctas(k_conv<CIN, COUT>);
   const int tiles = B * (H / TH) * (W / TW);
-  k_conv<CIN, COUT><<<tiles, kThreads, 0, st>>>(in, w, b, H, W, y, a, act, cout_store);
+  k_conv<CIN, COUT><<<std::min(tiles, ctas), kThreads, 0, st>>>(in, w, b, H, W, tiles, y, a, act, cout_store);
 }
 
 template <int CIN, int COUT>
@@ -431,13 +498,12 @@ struct r2d3c_cnn {
       const Layer& ly = L[l];
       // dY holds dL/dy of layer l (bf16, coutp channels)
       wgrad(l, act[l], dY, B);
-      const int kc = 9 * ly.cinp * ly.coutp;
+      // per-CTA partials: 9*cinp*coutp weight entries, then coutp bias entries
+      const int kc = 9 * ly.cinp * ly.coutp + ly.coutp;
       k_reduce_parts<<<(kc + 255) / 256, 256, 0, st>>>(part, nparts, kc, part + (size_t)nparts * kc);
       cuda_check(cudaGetLastError(), "k_reduce_parts");
-      // unpad into grad (layout [9][cin][cout])
+      // unpad into grad (layout [9][cin][cout], then the bias)
       unpad_wgrad(l, part + (size_t)nparts * kc);
-      k_bias_grad<<<ly.cout, 256, 0, st>>>(dY, npix, ly.coutp, grad + ly.boff);
-      cuda_check(cudaGetLastError(), "k_bias_grad");
       if (l == 0) break;
       // dA of layer l-1 = conv(dY, wb[l]); then dY' = dA * gelu'(pre[l-1])
       conv(l, dY, wb[l], B, nullptr, dA, 0, false, true);
@@ -454,8 +520,9 @@ struct r2d3c_cnn {
 
   void unpad_wgrad(int l, const float* gp) {
     const Layer& ly = L[l];
-    const int c = 9 * ly.cin * ly.cout;
-    k_unpad_wgrad<<<(c + 255) / 256, 256, 0, st>>>(gp, ly.cin, ly.cout, ly.cinp, ly.coutp, grad + ly.woff);
+    const int c = 9 * ly.cin * ly.cout + ly.cout;
+    k_unpad_wgrad<<<(c + 255) / 256, 256, 0, st>>>(gp, ly.cin, ly.cout, ly.cinp, ly.coutp, grad + ly.woff,
+                                                    grad + ly.boff);
     cuda_check(cudaGetLastError(), "k_unpad_wgrad");
   }
 
@@ -532,7 +599,7 @@ int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** out) {
     for (int l = 0; l < kLayers; ++l) c->act[l + 1] = c->alloc<bf16>(npix * kCoutPad[l]);
     c->dA = c->alloc<bf16>(npix * 32);
     c->dY = c->alloc<bf16>(npix * 32);  // dL/dy of the current layer (<= 32 channels)
-    c->part = c->alloc<float>((size_t)(c->nparts + 1) * 9 * 32 * 32);
+    c->part = c->alloc<float>((size_t)(c->nparts + 1) * (9 * 32 * 32 + 32));
     c->lpart = c->alloc<float>(256);
     c->norm = c->alloc<float>(20);
     const float ident[20] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 1, 1};
