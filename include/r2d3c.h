@@ -235,6 +235,16 @@ int r2d3c_cnn_set_normalization(r2d3c_cnn* cnn, const float* in_mean, const floa
 int r2d3c_closure_inputs(r2d3c_ctx* ctx, float* d_x);
 int r2d3c_closure_sample(r2d3c_ctx* fine, r2d3c_ctx* coarse, float* d_x, float* d_y);
 int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t);
+/* nsteps LES steps with the network in the loop: before every RK step the
+   8 inputs of the current state are formed, the network cnn (grid n x n) is
+   evaluated on them and its two outputs are added to the brackets of that
+   step.  All of it (inputs, network, tendencies, step) is captured as one
+   CUDA graph and replayed nsteps times, with dt from the CFL condition or
+   fixed as in r2d3c_advance; constant forcing only (iflow 0 or 1).  The
+   network's buffers are in use until the call returns; the tendencies are
+   switched off on return. */
+int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
+                          double* time, double* dt_last);
 
 /* ---- Level 2 operators (reference subroutines on host arrays) ---------- */
 /* derivk2 (pseudospec2D_Rot2D3C.f90:6-68) */

@@ -114,6 +114,7 @@ SIGNATURES = {
     "r2d3c_closure_inputs": (C.c_int, [_P, _P]),
     "r2d3c_closure_sample": (C.c_int, [_P, _P, _P, _P]),
     "r2d3c_closure_set_tendency": (C.c_int, [_P, _P]),
+    "r2d3c_closure_advance": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_double, _D, _D]),
     "r2d3c_derivk2": (C.c_int, [_P, _D, _D, C.c_int]),
     "r2d3c_laplak2": (C.c_int, [_P, _D, _D]),
     "r2d3c_inv_laplak2": (C.c_int, [_P, _D, _D]),

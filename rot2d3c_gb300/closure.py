@@ -84,3 +84,12 @@ def set_tendency(ctx, d_t) -> None:
     """Subgrid tendencies ([n, n, 2] FP32, physical) added to the brackets of
     the following steps of ctx; None switches them off."""
     check(load().r2d3c_closure_set_tendency(ctx._h, None if d_t is None else _ptr(d_t)), "closure_set_tendency")
+
+
+def closure_advance(ctx, net: CNN, nsteps: int, dt_mode: int, cfl_or_dt: float):
+    """nsteps LES steps of ctx with the network evaluated before every step
+    (one captured CUDA graph per step).  Returns (time, dt of the last step)."""
+    t, dtl = C.c_double(), C.c_double()
+    check(load().r2d3c_closure_advance(ctx._h, net._h, nsteps, dt_mode, cfl_or_dt, C.byref(t), C.byref(dtl)),
+          "closure_advance")
+    return t.value, dtl.value

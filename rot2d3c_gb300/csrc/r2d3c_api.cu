@@ -86,8 +86,21 @@ struct r2d3c_ctx {
   r2d3c_params p{};
   std::unique_ptr<IEngine> eng;
   int ci_final_seed = 0;  // seed value left by one const_inj call
+  // closure-graph scratch: network inputs [n][n][8] and tendencies [n][n][2]
+  float* cl_x = nullptr;
+  float* cl_t = nullptr;
   ModelCoef mc() const { return ModelCoef{p.nu, p.hnu, p.nuv, p.hnuv, p.omega, p.nn, p.mm, p.nnv, p.mmv}; }
+  ~r2d3c_ctx() {
+    eng.reset();
+    if (cl_x) cudaFree(cl_x);
+    if (cl_t) cudaFree(cl_t);
+  }
 };
+
+namespace r2d3c {
+void cnn_forward_on(r2d3c_cnn* c, const float* d_x, int batch, float* d_out, cudaStream_t stream);
+void cnn_shape(const r2d3c_cnn* c, int* H, int* W, int* max_batch, unsigned long long* serial);
+}  // namespace r2d3c
 
 struct r2d3c_plan {
   int n = 0, dir = 0;
@@ -944,7 +957,7 @@ int r2d3c_fp64_fma_peak(double* tflops) {
 int r2d3c_closure_inputs(r2d3c_ctx* ctx, float* d_x) {
   API_BEGIN
   REQUIRE(ctx && d_x, "NULL argument");
-  ctx->eng->closure_inputs(d_x);
+  ctx->eng->closure_inputs(d_x, true);
   API_END
 }
 
@@ -955,7 +968,7 @@ int r2d3c_closure_sample(r2d3c_ctx* fine, r2d3c_ctx* coarse, float* d_x, float* 
   IEngine* c = coarse->eng.get();
   c->coarsen_from(fine->eng.get(), P_PS, P_PS);
   c->coarsen_from(fine->eng.get(), P_VZ, P_VZ);
-  c->closure_inputs(d_x);
+  c->closure_inputs(d_x, true);
   c->closure_targets(fine->eng.get(), d_y);
   API_END
 }
@@ -963,7 +976,53 @@ int r2d3c_closure_sample(r2d3c_ctx* fine, r2d3c_ctx* coarse, float* d_x, float* 
 int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t) {
   API_BEGIN
   REQUIRE(ctx, "NULL argument");
-  ctx->eng->set_closure(d_t);
+  ctx->eng->set_closure(d_t, true);
+  API_END
+}
+
+int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
+                          double* time, double* dt_last) {
+  API_BEGIN
+  REQUIRE(ctx && cnn, "NULL argument");
+  REQUIRE(nsteps >= 0, "nsteps must be >= 0");
+  REQUIRE(dt_mode == R2D3C_DT_CFL || dt_mode == R2D3C_DT_FIXED, "bad dt_mode");
+  REQUIRE(cfl_or_dt > 0.0 && std::isfinite(cfl_or_dt), "cfl_or_dt must be positive and finite");
+  REQUIRE(ctx->p.iflow == 0 || ctx->p.iflow == 1, "the closure advance takes constant forcing (iflow 0 or 1)");
+  int H = 0, W = 0, bmax = 0;
+  unsigned long long serial = 0;
+  cnn_shape(cnn, &H, &W, &bmax, &serial);
+  const int n = ctx->p.n;
+  REQUIRE(H == n && W == n, "the network's grid must be the context's n x n");
+  IEngine* e = ctx->eng.get();
+  if (!ctx->cl_x) {
+    cuda_check(cudaMalloc(&ctx->cl_x, sizeof(float) * 8 * (size_t)n * n), "cudaMalloc closure inputs");
+    cuda_check(cudaMalloc(&ctx->cl_t, sizeof(float) * 2 * (size_t)n * n), "cudaMalloc closure tendencies");
+  }
+  cuda_check(cudaMemsetAsync(ctx->cl_t, 0, sizeof(float) * 2 * (size_t)n * n, (cudaStream_t)e->stream()),
+             "memset");
+  e->set_closure(ctx->cl_t, true);  // closure on; the hook refreshes the tendencies before every step
+  float* x = ctx->cl_x;
+  float* t = ctx->cl_t;
+  e->set_step_hook(
+      [e, cnn, x, t](cudaStream_t s) {
+        e->closure_inputs(x, false);
+        cnn_forward_on(cnn, x, 1, t, s);
+        e->set_closure(t, false);
+      },
+      serial);
+  try {
+    if (dt_mode == R2D3C_DT_FIXED) e->set_dt(cfl_or_dt);
+    e->advance(ctx->mc(), nsteps, dt_mode == R2D3C_DT_CFL, cfl_or_dt, nullptr);
+  } catch (...) {
+    e->set_step_hook(nullptr, 0);
+    e->set_closure(nullptr, true);
+    throw;
+  }
+  e->set_step_hook(nullptr, 0);
+  e->set_closure(nullptr, true);
+  if (time) *time = e->get_time();
+  if (dt_last) *dt_last = e->get_dt();
+  e->sync();
   API_END
 }
 

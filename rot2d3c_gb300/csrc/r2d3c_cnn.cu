@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -414,8 +415,7 @@ int resident_ctas(K k) {
 
 template <int CIN, int COUT>
 void conv_launch(const bf16* in, const bf16* w, const float* b, int B, int H, int W, float* y, bf16* a, int act,
-                 int cout_store, cudaStream_t st) {
-  static const int ctas = resident_ctas(k_conv<CIN, COUT>);
+                 int cout_store, int ctas, cudaStream_t st) {
   const int tiles = B * (H / TH) * (W / TW);
   k_conv<CIN, COUT><<<std::min(tiles, ctas), kThreads, 0, st>>>(in, w, b, H, W, tiles, y, a, act, cout_store);
 }
@@ -430,6 +430,8 @@ void wgrad_launch(const bf16* in, const bf16* dy, int B, int H, int W, float* pa
 
 struct r2d3c_cnn {
   int H = 0, W = 0, Bmax = 0;
+  unsigned long long serial = 0;  // unique per network created in this process
+  int ctas[3] = {};               // resident CTAs of k_conv<16,32>, <32,32>, <32,16>
   cudaStream_t st = nullptr;
   Layer L[kLayers];
   size_t nparam = 0;
@@ -462,9 +464,9 @@ struct r2d3c_cnn {
     // forward shapes (CINP, COUTP) or backward-data shapes (COUTP, CINP)
     const int ci = back ? L[l].coutp : L[l].cinp, co = back ? L[l].cinp : L[l].coutp;
     const int store = back ? co : (l == kLayers - 1 ? L[l].cout : co);
-    if (ci == 16 && co == 32) conv_launch<16, 32>(in, w, b, B, H, W, y, a, act_on, store, st);
-    else if (ci == 32 && co == 32) conv_launch<32, 32>(in, w, b, B, H, W, y, a, act_on, store, st);
-    else if (ci == 32 && co == 16) conv_launch<32, 16>(in, w, b, B, H, W, y, a, act_on, store, st);
+    if (ci == 16 && co == 32) conv_launch<16, 32>(in, w, b, B, H, W, y, a, act_on, store, ctas[0], st);
+    else if (ci == 32 && co == 32) conv_launch<32, 32>(in, w, b, B, H, W, y, a, act_on, store, ctas[1], st);
+    else if (ci == 32 && co == 16) conv_launch<32, 16>(in, w, b, B, H, W, y, a, act_on, store, ctas[2], st);
     else throw Error(kEINVAL, "unsupported conv shape");
     cuda_check(cudaGetLastError(), "k_conv");
   }
@@ -545,6 +547,31 @@ struct r2d3c_cnn {
   }
 };
 
+namespace r2d3c {
+// Forward of one batch queued on `stream` (no synchronisation; capturable):
+// the network's own buffers and weights, the output denormalised into d_out.
+void cnn_forward_on(r2d3c_cnn* c, const float* d_x, int batch, float* d_out, cudaStream_t stream) {
+  cudaStream_t own = c->st;
+  c->st = stream;
+  try {
+    c->forward(d_x, batch);
+    k_denorm<<<512, 256, 0, stream>>>(c->pre[kLayers - 1], (size_t)batch * c->H * c->W, c->norm + 16,
+                                      c->norm + 18, d_out);
+    cuda_check(cudaGetLastError(), "k_denorm");
+  } catch (...) {
+    c->st = own;
+    throw;
+  }
+  c->st = own;
+}
+void cnn_shape(const r2d3c_cnn* c, int* H, int* W, int* max_batch, unsigned long long* serial) {
+  *H = c->H;
+  *W = c->W;
+  *max_batch = c->Bmax;
+  *serial = c->serial;
+}
+}  // namespace r2d3c
+
 namespace {
 int fail(const Error& e) {
   last_error_slot() = e.what();
@@ -564,6 +591,11 @@ int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** out) {
     c->H = H;
     c->W = W;
     c->Bmax = max_batch;
+    static std::atomic<unsigned long long> next_serial{1};
+    c->serial = next_serial++;
+    c->ctas[0] = resident_ctas(k_conv<16, 32>);
+    c->ctas[1] = resident_ctas(k_conv<32, 32>);
+    c->ctas[2] = resident_ctas(k_conv<32, 16>);
     cuda_check(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate");
     size_t off = 0;
     for (int l = 0; l < kLayers; ++l) {

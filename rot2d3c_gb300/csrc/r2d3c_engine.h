@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -103,11 +104,16 @@ class IEngine {
   // (physical, FP32 NHWC [n][n][8]); the subgrid targets against a finer run
   // (FP32 NHWC [n][n][2]); the tendencies added to the two brackets by the
   // following steps (physical FP32 [n][n][2]; null switches them off)
-  virtual void closure_inputs(float* d_x) = 0;
+  // (wait = false: queue the work and return, for capture into a graph)
+  virtual void closure_inputs(float* d_x, bool wait) = 0;
   virtual void brackets() = 0;  // [psi,-k^2 psi] -> P_B5, [psi,vz] -> P_B6 (full plane)
   virtual void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) = 0;
   virtual void closure_targets(IEngine* fine, float* d_y) = 0;
-  virtual void set_closure(const float* d_t) = 0;
+  virtual void set_closure(const float* d_t, bool wait) = 0;
+  // Work queued on the engine stream before every step of advance(), inside
+  // the captured graph (id != 0; id identifies the hook for the graph cache,
+  // and id 0 removes it).
+  virtual void set_step_hook(std::function<void(cudaStream_t)> hook, unsigned long long id) = 0;
   virtual void rand_force(const RandForceHost f[2]) = 0;
   // One RK4 step.  cfl_mode: dt from the CFL condition of the current state
   // (fused into the first substep), else the dt already set.  add_time:

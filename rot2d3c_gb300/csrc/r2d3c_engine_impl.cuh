@@ -438,7 +438,7 @@ class EngineT final : public IEngine {
       sync();  // seq goes out of scope
     }
     upload_coefs(mc, cfl);
-    GraphKey key{cfl_mode, rf != nullptr, closure_on_};
+    GraphKey key{cfl_mode, rf != nullptr, closure_on_, hook_ ? hook_id_ : 0ull};
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
@@ -446,6 +446,7 @@ class EngineT final : public IEngine {
       const int before = launches_;
       cuda_check(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal), "BeginCapture");
       try {
+        if (hook_) hook_(st_);
         enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr);
       } catch (...) {
         cudaStreamEndCapture(st_, &g);
@@ -536,14 +537,19 @@ class EngineT final : public IEngine {
   // device arrays read by the kernels, so changing them needs no recapture.
   struct GraphKey {
     bool cfl_mode = false, rf = false, closure = false;
+    unsigned long long hook = 0;
     bool same(const GraphKey& o) const {
-      return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure;
+      return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure && hook == o.hook;
     }
   };
   static bool batched(int p) { return p <= P_C2; }  // ps, vz, fp, fz, c1, c2
 
  public:
-  void closure_inputs(float* d_x) override {
+  void set_step_hook(std::function<void(cudaStream_t)> hook, unsigned long long id) override {
+    hook_ = id ? std::move(hook) : nullptr;
+    hook_id_ = id;
+  }
+  void closure_inputs(float* d_x, bool wait) override {
     const size_t cnt = (size_t)n_ * n_;
     const double s = 1.0 / ((double)n_ * n_);
     // omega = -lap psi = k^2 psi: -(laplak2 psi); vz; d/dx, d/dy of psi, omega, vz
@@ -559,7 +565,7 @@ class EngineT final : public IEngine {
       k_to_channel<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_1], cnt, ch[c].sign * s, d_x, 8, c);
       post("k_to_channel");
     }
-    sync();
+    if (wait) sync();
   }
   void brackets() override { brackets_full(); }
   void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) override {
@@ -586,7 +592,7 @@ class EngineT final : public IEngine {
     }
     sync();
   }
-  void set_closure(const float* d_t) override {
+  void set_closure(const float* d_t, bool wait) override {
     if (!d_t) {
       closure_on_ = false;
       return;
@@ -601,7 +607,7 @@ class EngineT final : public IEngine {
     // the tendency planes are fixed buffers: a captured step keyed on
     // closure_on_ stays valid across calls
     closure_on_ = true;
-    sync();
+    if (wait) sync();
   }
 
  private:
@@ -942,6 +948,8 @@ class EngineT final : public IEngine {
   bool full_;
   int nb_ = 1, run_ = 0;
   bool closure_on_ = false;
+  std::function<void(cudaStream_t)> hook_;
+  unsigned long long hook_id_ = 0;
   int pipeb_ctas_ = 0;  // resident CTAs of the pipelined pass B (whole device)
   cpx<T>* pbase_[P_COUNT] = {};
   double* scal_base_ = nullptr;
