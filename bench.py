@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--err-steps", type=int, default=100)
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-steps", type=int, default=500)
+    ap.add_argument("--no-closure", action="store_true")
     return ap.parse_args()
 
 
@@ -339,6 +340,29 @@ def run_ensemble(args, torch):
     return out
 
 
+# ---------------------------------------------------------------- closure
+CLOSURE = dict(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=10, spinup=2000, train_steps=3000,
+               batch=32, lr=1e-3, les_steps=4000, cfl=0.5, seed=1)
+
+
+def run_closure():
+    """The learned-closure experiment (rot2d3c_gb300.les): FP32 DNS at 2048^2,
+    filtered snapshots, CNN training, then the 256^2 LES with the network in
+    the loop against the plain and hyperviscous coarse solvers and the
+    filtered DNS over the same physical time.  The gain is the DNS's GPU
+    seconds over the LES's for that time."""
+    from rot2d3c_gb300.les import run_experiment
+    r = run_experiment(**CLOSURE)
+    tr = r["training"]
+    return {"les_vs_dns_gain": r["les"]["gain"], "unit": "DNS GPU-s / LES GPU-s (same physical time)",
+            "dns": r["dns"], "les": r["les"], "spectrum_error": r["spectrum_error"],
+            "training": dict(tr, ms_per_step=1e3 * tr["train_s"] / tr["steps"],
+                             samples_per_s=tr["steps"] * tr["batch"] / tr["train_s"]),
+            "config": dict(CLOSURE, network="6 x conv3x3 8-32-32-32-32-32-2, GELU, BF16 tensor-core MMA, FP32 master "
+                                           "weights, Adam; dataset and LES on GPU"),
+            "total_s": r["total_s"]}
+
+
 # ---------------------------------------------------------------- CPU legs
 def cpu_baseline(n, ps, vz, fp, fz, budget_s=20.0):
     """The C/OpenMP restatement of the reference step (oracle/cpu) on all host
@@ -520,6 +544,9 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n, ps, vz, fp, fz)
+    closure = None
+    if rank == 0 and world == 1 and not args.no_closure:
+        closure = run_closure()
 
     line = {"metric": METRIC, "value": v32, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": 1e3 * el32 / K, "higher_is_better": True, "scaling": "weak",
@@ -530,7 +557,7 @@ def main():
                        "l2": "working set larger than L2 (6 mixed planes of 268 MB at 4096^2 FP32)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches32, "roofline": roofline, "clocks": clocks, "e2e": e2e,
-            "fp64": fp64, "ensemble": ensemble, "cpu_baseline": cpu}
+            "fp64": fp64, "ensemble": ensemble, "closure": closure, "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
     c32.destroy()

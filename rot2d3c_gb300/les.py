@@ -153,6 +153,11 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
         runs[name] = c
     spectra = {k: [] for k in runs}
     spectra["dns"] = []
+    fluxes = {k: [] for k in spectra}
+
+    def flux(c):  # running sum of the total energy transfer (2-D part + vz part)
+        _, f1, f2 = c.transfers()
+        return np.cumsum(f1 + f2)
     xbuf = torch.empty((1, nc, nc, 8), dtype=torch.float32, device="cuda")
     tbuf = torch.empty((1, nc, nc, 2), dtype=torch.float32, device="cuda")
     # initial coarse state = filtered DNS state (through one closure sample)
@@ -172,6 +177,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
         t_les, _ = closure_advance(les, net, spec_every, DT_CFL, cfl)
         if s + spec_every > les_steps // 2:
             spectra["les"].append(les.spectrum()[0])
+            fluxes["les"].append(flux(les))
     torch.cuda.synchronize()
     t_les_gpu = time.perf_counter() - t0
     T = t_les - t_dns0
@@ -181,6 +187,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
             c.advance(spec_every, DT_CFL, cfl)
             if s + spec_every > les_steps // 2:
                 spectra[name].append(c.spectrum()[0])
+                fluxes[name].append(flux(c))
     # DNS over the same physical time; filtered spectrum sampled on the same
     # cadence in time
     torch.cuda.synchronize()
@@ -195,6 +202,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
         if td >= nxt:
             closure_sample(fine, coarse, xbuf[0], tbuf[0])
             spectra["dns"].append(coarse.spectrum()[0])
+            fluxes["dns"].append(flux(fine))
             nxt += dT
     torch.cuda.synchronize()
     t_dns_gpu = time.perf_counter() - t0
@@ -212,6 +220,10 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
             # the top third of the resolved shells, where the closure acts
             "rel_l1_top_third": float(np.sum(np.abs(d - r)[2 * len(r) // 3:]) / np.sum(r[2 * len(r) // 3:])),
         }
+        # energy flux through k (resolved transfers) against the DNS's, 1 <= k < k_c
+        fl = np.mean(fluxes[name], axis=0)[1:kc]
+        fr = np.mean(fluxes["dns"], axis=0)[1:kc]
+        err[name]["flux_rel_l1"] = float(np.sum(np.abs(fl - fr)) / max(np.sum(np.abs(fr)), 1e-300))
     return {
         "dns": {"n": nf, "steps_compared": dns_steps, "gpu_s": t_dns_gpu, "physical_time": T},
         "les": {"n": nc, "steps": les_steps, "gpu_s": t_les_gpu, "gain": t_dns_gpu / t_les_gpu},

@@ -57,3 +57,28 @@ def test_fp32_batched_equals_single(gpu, n):
         np.testing.assert_array_equal(eb, b)
         assert times[i] == t
     ens.destroy()
+
+
+def test_fp32_vs_fp64_at_8192_spectra(gpu):
+    """8192^2, 50 CFL steps (nu = 2e-6, Omega = 1, IC k^-3 on 1 <= |k| <= 200,
+    forcing shell 30-32): the FP32 path against the FP64 path, per field and
+    per shell of the energy spectrum."""
+    n = 8192
+    _, cp = params(n, omega=1.0, nu=2e-6, nuv=2e-6, hnu=0.1, hnuv=0.1, iflow=0)
+    g, ps, vz = random_state(n, 81, kmax_shell=200.0, slope=-3.0, amp=float(n) ** 2)
+    fp, fz = random_forcing(g, 82, 30.0, 32.0)
+    out = {}
+    for prec in (0, 1):
+        c = gpu.Context(cp, prec)
+        c.set_state(ps, vz)
+        c.set_forcing(fp, fz)
+        c.set_time(0.0)
+        c.advance(50, gpu.DT_CFL, 0.5)
+        out[prec] = (c.get_state(), c.spectrum()[0])
+        c.destroy()
+    (a64, b64), ek64 = out[0]
+    (a32, b32), ek32 = out[1]
+    assert rel_l2(a32, a64) < 2e-5
+    assert rel_l2(b32, b64) < 2e-5
+    live = ek64 > 1e-12 * ek64.max()
+    assert np.max(np.abs(ek32[live] - ek64[live]) / ek64[live]) < 1e-3
