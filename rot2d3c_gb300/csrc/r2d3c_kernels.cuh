@@ -915,7 +915,98 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   // read only now, not held in registers across the transforms.
   const StepCoef sc = scs[blockIdx.y];
   const T tmp1 = (T)(scal[blockIdx.y * kScalStride] / (double)o);  // :581
-  if constexpr (HOLD) {
+  if constexpr (HOLD && sizeof(T) == 4) {
+    // FP32: c6 joins c5 in shared memory (the transform buffer is free after
+    // the last transform), then the threads update the retained rows two at a
+    // time (rows 2p, 2p+1 of one column: 16-byte loads and stores), two row
+    // pairs per iteration with all loads of an iteration issued before its
+    // stores.  Each element is still loaded and stored by one thread.
+    cpx<T>* c6s = sm;
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) c6s[t * N + lane + q * C::TPF] = v[t][q];
+    __syncthreads();
+    const int L = gd.L;
+    const int lo_pairs = L / 2 + 1;       // pairs p = 0 .. L/2 hold rows 0 .. L
+    const int hi_first = (N - L) / 2;     // pairs hi_first .. N/2-1 hold rows N-L .. N-1
+    const int npc = lo_pairs + (N / 2 - hi_first);
+    const int total = NT * npc;
+    using F4 = float4;
+    constexpr int RB = 2;
+    auto ld4 = [](const cpx<T>* base, size_t idx) { return *reinterpret_cast<const F4*>(base + idx); };
+#pragma unroll 1
+    for (int e0 = lane; e0 < total; e0 += RB * C::TPF) {
+      F4 a1[RB], a2[RB], p0[RB], f0[RB], v0[RB], g0[RB];
+      int col[RB], j0[RB];
+      bool keep[RB][2], in[RB][2];
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const int e = e0 + b * C::TPF;
+        const int t = e / npc, pi = e % npc;
+        const int pr = pi < lo_pairs ? pi : hi_first + (pi - lo_pairs);
+        col[b] = kx0 + t;
+        j0[b] = 2 * pr;
+        bool any = false;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int ky = ky_of(j0[b] + h, N), k2 = col[b] * col[b] + ky * ky;
+          keep[b][h] = e < total && col[b] < gd.M && ky <= L && -ky <= L;
+          in[b][h] = keep[b][h] && k2 <= gd.kmaxi && k2 >= 1;
+          any |= in[b][h];
+        }
+        if (any) {
+          const size_t idx = (size_t)col[b] * N + j0[b];
+          a1[b] = ld4(c1in, idx);
+          a2[b] = ld4(c2in, idx);
+          p0[b] = ld4(ps, idx);
+          f0[b] = ld4(fp, idx);
+          v0[b] = ld4(vz, idx);
+          g0[b] = ld4(fz, idx);
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        if (!keep[b][0] && !keep[b][1]) continue;
+        const int t = col[b] - kx0;
+        const size_t idx = (size_t)col[b] * N + j0[b];
+        // the two rows of the pair: h = 0 (x, y halves of the float4s), h = 1 (z, w)
+        auto row = [&](int h, cpx<T>& n1, cpx<T>& n2) {
+          n1 = czero<T>();
+          n2 = czero<T>();
+          if (!in[b][h]) return;
+          const int ky = ky_of(j0[b] + h, N), k2 = col[b] * col[b] + ky * ky;
+          RkIn<T> r;
+          r.a1 = h ? mkc<T>(a1[b].z, a1[b].w) : mkc<T>(a1[b].x, a1[b].y);
+          r.a2 = h ? mkc<T>(a2[b].z, a2[b].w) : mkc<T>(a2[b].x, a2[b].y);
+          r.p0 = h ? mkc<T>(p0[b].z, p0[b].w) : mkc<T>(p0[b].x, p0[b].y);
+          r.f0 = h ? mkc<T>(f0[b].z, f0[b].w) : mkc<T>(f0[b].x, f0[b].y);
+          r.v0 = h ? mkc<T>(v0[b].z, v0[b].w) : mkc<T>(v0[b].x, v0[b].y);
+          r.g0 = h ? mkc<T>(g0[b].z, g0[b].w) : mkc<T>(g0[b].x, g0[b].y);
+          cpx<T> c5 = hold[t * N + j0[b] + h], c6 = c6s[t * N + j0[b] + h];
+          if (tau5) {  // learned subgrid tendencies of the two brackets
+            const cpx<T> u = tau5[idx + h], w = tau6[idx + h];
+            c5 = mkc<T>(c5.x + u.x, c5.y + u.y);
+            c6 = mkc<T>(c6.x + w.x, c6.y + w.y);
+          }
+          rk_apply<T>(r, c5, c6, ky, k2, sc, tmp1, n1, n2);
+        };
+        cpx<T> n10, n20, n11, n21;
+        row(0, n10, n20);
+        row(1, n11, n21);
+        if (keep[b][0] && keep[b][1]) {
+          *reinterpret_cast<F4*>(c1out + idx) = make_float4(n10.x, n10.y, n11.x, n11.y);
+          *reinterpret_cast<F4*>(c2out + idx) = make_float4(n20.x, n20.y, n21.x, n21.y);
+        } else if (keep[b][0]) {
+          c1out[idx] = n10;
+          c2out[idx] = n20;
+        } else {
+          c1out[idx + 1] = n11;
+          c2out[idx + 1] = n21;
+        }
+      }
+    }
+  } else if constexpr (HOLD) {
     // c6 joins c5 in shared memory (the transform buffer is free after the
     // last transform; each thread reads back only what it wrote), and the
     // update runs over this thread's elements in batches of RB: all loads of
