@@ -146,7 +146,12 @@ __device__ __forceinline__ void fft_sync() {
 // complex buffers of SMEM_ELEMS elements, padded by one element every
 // 128 bytes so that the strided Stockham writes stay (nearly) bank-conflict
 // free.
-template <typename T, int N, int E, int NT = 1>
+//
+// Two FP32 transforms (NT = 2) are interleaved in shared memory instead
+// (unless ILV_OK is false): one float4 per position holds both transforms'
+// values, so every exchange moves 16 bytes per instruction (half the
+// shared-memory instructions), padded by one float4 every 128 bytes.
+template <typename T, int N, int E, int NT = 1, bool ILV_OK = true>
 struct BlockFFT {
   static_assert((N & (N - 1)) == 0 && N >= E && E >= 2, "N, E powers of two");
   static constexpr int TPF = N / E;
@@ -154,11 +159,21 @@ struct BlockFFT {
   static constexpr int LOGE = ilog2(E);
   static constexpr int NST = (LOGN + LOGE - 1) / LOGE;
   static constexpr int LAST_R = 1 << (LOGN - LOGE * (NST - 1));
-  static constexpr int PADSH = ilog2(128 / (int)sizeof(cpx<T>));
-  static constexpr int SMEM_ELEMS = N + (N >> PADSH);  // per transform
+  static constexpr bool ILV = ILV_OK && sizeof(T) == 4 && NT == 2;  // interleaved float4 exchange
+  static constexpr int PADSH = ilog2(128 / (int)(ILV ? 16 : sizeof(cpx<T>)));
+  static constexpr int SMEM_ELEMS = N + (N >> PADSH);  // per transform (complex elements)
   static constexpr size_t SMEM_BYTES = (size_t)NT * SMEM_ELEMS * sizeof(cpx<T>);
 
   static __device__ __forceinline__ int pad(int i) { return i + (i >> PADSH); }
+  // both transforms' values at (padded) position idx of the interleaved layout
+  static __device__ __forceinline__ void st2(cpx<T>* sm, int idx, const cpx<T>& a, const cpx<T>& b) {
+    reinterpret_cast<float4*>(sm)[idx] = make_float4(a.x, a.y, b.x, b.y);
+  }
+  static __device__ __forceinline__ void ld2(const cpx<T>* sm, int idx, cpx<T>& a, cpx<T>& b) {
+    const float4 w = reinterpret_cast<const float4*>(sm)[idx];
+    a = mkc<T>(w.x, w.y);
+    b = mkc<T>(w.z, w.w);
+  }
 
   // Radix of stage s, sub-transform size NS before stage s, and the offset of
   // stage s's block in the stage-major twiddle table.  Block s holds the
@@ -215,16 +230,24 @@ struct BlockFFT {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int idx = pad(base + r * NS);
+          if constexpr (ILV) {
+            st2(sm, idx, v[0][m + r * B], v[NT - 1][m + r * B]);
+          } else {
 #pragma unroll
-          for (int t = 0; t < NT; ++t) sm[t * SMEM_ELEMS + idx] = v[t][m + r * B];
+            for (int t = 0; t < NT; ++t) sm[t * SMEM_ELEMS + idx] = v[t][m + r * B];
+          }
         }
       }
       fft_sync<TPF>();
 #pragma unroll
       for (int q = 0; q < E; ++q) {
         const int idx = pad(lane + q * TPF);
+        if constexpr (ILV) {
+          ld2(sm, idx, v[0][q], v[NT - 1][q]);
+        } else {
 #pragma unroll
-        for (int t = 0; t < NT; ++t) v[t][q] = sm[t * SMEM_ELEMS + idx];
+          for (int t = 0; t < NT; ++t) v[t][q] = sm[t * SMEM_ELEMS + idx];
+        }
       }
       fft_sync<TPF>();
       stage<DIR, S + 1, NS * R>(v, lane, sm, tw);
@@ -244,12 +267,21 @@ struct BlockFFT {
 #pragma unroll
     for (int q = 0; q < E; ++q) {
       const int idx = pad(lane + q * TPF);
+      if constexpr (ILV) {
+        st2(sm, idx, v[0][q], v[NT - 1][q]);
+      } else {
 #pragma unroll
-      for (int t = 0; t < NT; ++t) sm[t * SMEM_ELEMS + idx] = v[t][q];
+        for (int t = 0; t < NT; ++t) sm[t * SMEM_ELEMS + idx] = v[t][q];
+      }
     }
   }
   static __device__ __forceinline__ cpx<T> from_smem(int t, int k, const cpx<T>* sm) {
-    return sm[t * SMEM_ELEMS + pad(k)];
+    if constexpr (ILV) {
+      const float4 w = reinterpret_cast<const float4*>(sm)[pad(k)];
+      return t ? mkc<T>(w.z, w.w) : mkc<T>(w.x, w.y);
+    } else {
+      return sm[t * SMEM_ELEMS + pad(k)];
+    }
   }
 };
 

@@ -50,10 +50,10 @@ constexpr int kScalStride = 8;
 
 // Launch shape of a kernel carrying NT transforms per thread group: E
 // elements per thread, TPF = N/E threads per transform group, G groups per CTA.
-template <typename T, int N, int NT = 1, int EOVR = 0>
+template <typename T, int N, int NT = 1, int EOVR = 0, bool ILV_OK = true>
 struct Cfg {
   static constexpr int E = EOVR ? EOVR : (N >= 8192 ? 16 : 8);
-  using FFT = BlockFFT<T, N, E, NT>;
+  using FFT = BlockFFT<T, N, E, NT, ILV_OK>;
   static constexpr int TPF = N / E;
   static constexpr int G = TPF >= 256 ? 1 : 256 / TPF;  // transform groups per CTA
   static constexpr int THREADS = TPF * G;
@@ -77,8 +77,10 @@ template <typename T, int N> struct PassNT {
 template <typename T, int N> struct PassAE {
   static constexpr int value = (sizeof(T) == 4 && N == 4096) ? 16 : Cfg<T, N>::E;
 };
+// (pass A keeps the two transforms' exchange buffers separate: with its 255
+// registers the interleaved float4 exchange measured slower)
 template <typename T, int N>
-using CfgA = Cfg<T, N, PassNT<T, N>::value, PassAE<T, N>::value>;
+using CfgA = Cfg<T, N, PassNT<T, N>::value, PassAE<T, N>::value, PassAE<T, N>::value != 16>;
 
 // Shared memory of passes B and C: NT transform buffers per group, plus (when
 // it fits) a store for the first transform's result, which is held across the
