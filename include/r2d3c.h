@@ -246,6 +246,19 @@ int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t);
 int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
                           double* time, double* dt_last);
 
+/* ---- Regridding (regrid_slices.f90) ------------------------------------ */
+/* The reference's slice regridder applied to a whole field
+   (regrid_slices.f90:95-104): out(j,k) = in((j+1)*n/m, (k+1)*n/m) with
+   1-based indices and integer division, in R(n,n), out R(m,m), host FP64
+   buffers; n < m <= 2n (the map reads outside the field beyond 2n). */
+int r2d3c_regrid_physical(int n, int m, const double* in, double* out);
+/* the same on device buffers, queued on `stream` */
+int r2d3c_regrid_physical_dev(int n, int m, const double* d_in, double* d_out, void* stream);
+/* No reference counterpart: spectral zero-padding of src's state (ps, vz)
+   onto the finer grid of dst (modes |kx|,|ky| < n_src/2, scaled by
+   (n_dst/n_src)^2 so that the physical fields agree on the common points). */
+int r2d3c_regrid_spectral(r2d3c_ctx* src, r2d3c_ctx* dst);
+
 /* ---- Level 2 operators (reference subroutines on host arrays) ---------- */
 /* derivk2 (pseudospec2D_Rot2D3C.f90:6-68) */
 int r2d3c_derivk2(r2d3c_ctx* ctx, const double* a, double* b, int dir);
@@ -290,6 +303,12 @@ int r2d3c_fp64_fma_peak(double* tflops);
    which = 0 ps, 1 vz, 2 fp, 3 fz (spectral planes of the context's compute
    type, complex interleaved [kx][ky]). */
 int r2d3c_dev_ptr(r2d3c_ctx* ctx, int which, void** ptr);
+/* The plan chosen when the context was created (the counterpart of FFTW's
+   measured plans, fftp2D.f90:54-56): each launch-schedule variant of the
+   bracket pass that computes bit-identical results is timed on this GPU and
+   the fastest kept.  JSON text of the timings and the choice, NUL-terminated
+   in buf (R2D3C_EINVAL if len is too small). */
+int r2d3c_plan_report(r2d3c_ctx* ctx, char* buf, int len);
 /* The context's CUDA stream (cudaStream_t). */
 int r2d3c_stream(r2d3c_ctx* ctx, void** stream);
 /* Block until all queued work of the context is done. */

@@ -570,3 +570,30 @@ def closure_targets(gf: Grid, gc: Grid, psf, vzf) -> np.ndarray:
     t6 = coarsen(gf, gc, poisson(gf, psf, vzf)) - poisson(gc, psc, vzc)
     n2 = float(gc.n) ** 2
     return np.stack([c2r(gc, t5) / n2, c2r(gc, t6) / n2], axis=-1)
+
+
+# ---------------------------------------------------------------------------
+# regrid_slices.f90 (a stand-alone program of the reference)
+# ---------------------------------------------------------------------------
+def regrid_slices(vold: np.ndarray, n: int, m: int, nnodes: int, mnodes: int) -> np.ndarray:
+    """The reference's slice loops restated literally (regrid_slices.f90:62-115):
+    the n x n field is split into nnodes slices of ns = n/nnodes columns
+    (Fortran Vold(n, ns), x fastest), each old slice gives mnodes/nnodes new
+    slices of ms = m/mnodes columns, Vnew(j, k) = Vold((j+1)*n/m,
+    (k+(is-1)*ms+1)*n/m) with 1-based indices and integer division.  Input and
+    output are row-major [y][x] (= Fortran R(x, y)); the new slices are
+    concatenated in file order."""
+    ns, ms = n // nnodes, m // mnodes
+    out = np.empty((m, m))
+    for inode in range(nnodes):
+        vold_s = vold[inode * ns:(inode + 1) * ns, :]  # [k][j] = Vold(j, k)
+        for is_ in range(1, mnodes // nnodes + 1):
+            vnew = np.empty((ms, m))
+            for k in range(1, ms + 1):
+                k2 = (k + (is_ - 1) * ms + 1) * n // m
+                for j in range(1, m + 1):
+                    j2 = (j + 1) * n // m
+                    vnew[k - 1, j - 1] = vold_s[k2 - 1, j2 - 1]
+            slot = inode * (mnodes // nnodes) + is_ - 1
+            out[slot * ms:(slot + 1) * ms, :] = vnew
+    return out

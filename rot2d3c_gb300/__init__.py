@@ -63,6 +63,22 @@ def randu(seed: list) -> float:
     return float(np.float32(r))
 
 
+def regrid_physical(old: np.ndarray, m: int) -> np.ndarray:
+    """The reference's slice regridder (regrid_slices.f90:95-104) on a whole
+    n x n field (row-major [y][x]) onto m x m, n < m <= 2n."""
+    old = np.ascontiguousarray(old, np.float64)
+    n = old.shape[0]
+    assert old.shape == (n, n)
+    out = np.empty((m, m))
+    check(load().r2d3c_regrid_physical(n, m, _dptr(old), _dptr(out)), "regrid_physical")
+    return out
+
+
+def regrid_spectral(src: "Context", dst: "Context") -> None:
+    """dst's state = src's state zero-padded onto dst's finer grid."""
+    check(load().r2d3c_regrid_spectral(src._h, dst._h), "regrid_spectral")
+
+
 def fp64_fma_peak() -> float:
     """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
     t = C.c_double()
@@ -299,6 +315,13 @@ class Context:
         c = C.c_longlong()
         check(load().r2d3c_kernel_launches(self._h, C.byref(c)), "kernel_launches")
         return c.value
+
+    def plan_report(self) -> dict:
+        """The launch-schedule autotuner's timings and choice (r2d3c_plan_report)."""
+        import json
+        buf = C.create_string_buffer(4096)
+        check(load().r2d3c_plan_report(self._h, buf, len(buf)), "plan_report")
+        return json.loads(buf.value.decode())
 
     def device_bytes(self) -> int:
         c = C.c_longlong()

@@ -115,6 +115,10 @@ SIGNATURES = {
     "r2d3c_closure_sample": (C.c_int, [_P, _P, _P, _P]),
     "r2d3c_closure_set_tendency": (C.c_int, [_P, _P]),
     "r2d3c_closure_advance": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_double, _D, _D]),
+    "r2d3c_regrid_physical": (C.c_int, [C.c_int, C.c_int, _D, _D]),
+    "r2d3c_regrid_physical_dev": (C.c_int, [C.c_int, C.c_int, _P, _P, _P]),
+    "r2d3c_regrid_spectral": (C.c_int, [_P, _P]),
+    "r2d3c_plan_report": (C.c_int, [_P, C.c_char_p, C.c_int]),
     "r2d3c_derivk2": (C.c_int, [_P, _D, _D, C.c_int]),
     "r2d3c_laplak2": (C.c_int, [_P, _D, _D]),
     "r2d3c_inv_laplak2": (C.c_int, [_P, _D, _D]),

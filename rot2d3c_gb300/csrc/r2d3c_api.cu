@@ -973,6 +973,73 @@ int r2d3c_closure_sample(r2d3c_ctx* fine, r2d3c_ctx* coarse, float* d_x, float* 
   API_END
 }
 
+}  // extern "C"
+
+namespace {
+// The reference's slice regridder (regrid_slices.f90:95-104) on a whole
+// field: out(j, k) = in((j+1)*n/m, (k+1)*n/m) in 1-based Fortran indices
+// with integer division, out m x m, in n x n (n < m <= 2n).  Column-major
+// R(x, y) = row-major [y][x].
+__global__ void k_regrid_phys(const double* __restrict__ in, int n, double* __restrict__ out, int m) {
+  const size_t total = (size_t)m * m;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const long long y = (long long)(idx / m), x = (long long)(idx % m);
+    const long long sx = (x + 2) * n / m - 1, sy = (y + 2) * n / m - 1;  // 0-based
+    out[idx] = in[sy * n + sx];
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int r2d3c_regrid_spectral(r2d3c_ctx* src, r2d3c_ctx* dst) {
+  API_BEGIN
+  REQUIRE(src && dst, "NULL argument");
+  REQUIRE(dst->p.n > src->p.n, "the destination grid must be finer than the source grid");
+  REQUIRE(src->eng->precision() == dst->eng->precision(), "both contexts must have the same precision");
+  src->eng->sync();
+  IEngine* e = dst->eng.get();
+  e->refine_from(src->eng.get(), P_PS, P_PS);
+  e->refine_from(src->eng.get(), P_VZ, P_VZ);
+  e->mark_state_untruncated();
+  e->sync();
+  API_END
+}
+
+int r2d3c_regrid_physical_dev(int n, int m, const double* d_in, double* d_out, void* stream) {
+  API_BEGIN
+  REQUIRE(d_in && d_out, "NULL argument");
+  REQUIRE(n >= 1 && m > n && m <= 2 * n, "sizes must satisfy n < m <= 2n");
+  const size_t total = (size_t)m * m;
+  const int blocks = (int)std::min<size_t>((total + 255) / 256, 65535);
+  k_regrid_phys<<<blocks, 256, 0, (cudaStream_t)stream>>>(d_in, n, d_out, m);
+  cuda_check(cudaGetLastError(), "k_regrid_phys");
+  API_END
+}
+
+int r2d3c_regrid_physical(int n, int m, const double* in, double* out) {
+  API_BEGIN
+  REQUIRE(in && out, "NULL argument");
+  REQUIRE(n >= 1 && m > n && m <= 2 * n, "sizes must satisfy n < m <= 2n");
+  double *d_in = nullptr, *d_out = nullptr;
+  const size_t bi = sizeof(double) * (size_t)n * n, bo = sizeof(double) * (size_t)m * m;
+  cudaError_t err = cudaMalloc(&d_in, bi);
+  if (err == cudaSuccess) err = cudaMalloc(&d_out, bo);
+  if (err == cudaSuccess) err = cudaMemcpy(d_in, in, bi, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) {
+    const size_t total = (size_t)m * m;
+    k_regrid_phys<<<(int)std::min<size_t>((total + 255) / 256, 65535), 256>>>(d_in, n, d_out, m);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = cudaMemcpy(out, d_out, bo, cudaMemcpyDeviceToHost);
+  if (d_in) cudaFree(d_in);
+  if (d_out) cudaFree(d_out);
+  cuda_check(err, "regrid_physical");
+  API_END
+}
+
 int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t) {
   API_BEGIN
   REQUIRE(ctx, "NULL argument");
@@ -1023,6 +1090,17 @@ int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mod
   if (time) *time = e->get_time();
   if (dt_last) *dt_last = e->get_dt();
   e->sync();
+  API_END
+}
+
+int r2d3c_plan_report(r2d3c_ctx* ctx, char* buf, int len) {
+  API_BEGIN
+  REQUIRE(ctx && buf && len > 0, "NULL argument");
+  const std::string r = ctx->eng->plan_report();
+  const size_t k = std::min(r.size(), (size_t)len - 1);
+  std::memcpy(buf, r.data(), k);
+  buf[k] = 0;
+  REQUIRE(r.size() < (size_t)len, "buffer too small for the report");
   API_END
 }
 

@@ -483,6 +483,27 @@ __global__ void k_coarsen(const cpx<T>* __restrict__ fine, int nf, cpx<T>* __res
   }
 }
 
+// Spectral zero-padding onto a finer grid (the inverse of k_coarsen): every
+// mode |kx|, |ky| < nc/2 of the coarse plane lands at the same wavenumber of
+// the fine plane, times scale = (nf/nc)^2 (unnormalised transforms keep the
+// physical amplitude); all other fine modes are zero.
+template <typename T>
+__global__ void k_refine(const cpx<T>* __restrict__ coarse, int nc, cpx<T>* __restrict__ fine, DevGrid gf,
+                         double scale) {
+  const size_t total = (size_t)gf.nh * gf.n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / gf.n), j = (int)(idx % gf.n);
+    const int ky = ky_of(j, gf.n);
+    cpx<T> v = czero<T>();
+    if (i < nc / 2 && ky < nc / 2 && -ky < nc / 2) {
+      const cpx<T> c = coarse[(size_t)i * nc + (ky >= 0 ? ky : nc + ky)];
+      v = mkc<T>((T)(c.x * scale), (T)(c.y * scale));
+    }
+    fine[idx] = v;
+  }
+}
+
 // c = a - b on spectral planes
 template <typename T>
 __global__ void k_spec_sub(const cpx<T>* __restrict__ a, const cpx<T>* __restrict__ b, cpx<T>* __restrict__ c,

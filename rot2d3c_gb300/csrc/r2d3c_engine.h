@@ -108,6 +108,7 @@ class IEngine {
   virtual void closure_inputs(float* d_x, bool wait) = 0;
   virtual void brackets() = 0;  // [psi,-k^2 psi] -> P_B5, [psi,vz] -> P_B6 (full plane)
   virtual void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) = 0;
+  virtual void refine_from(IEngine* coarse, int coarse_plane, int dst_plane) = 0;  // spectral zero-pad
   virtual void closure_targets(IEngine* fine, float* d_y) = 0;
   virtual void set_closure(const float* d_t, bool wait) = 0;
   // Work queued on the engine stream before every step of advance(), inside
@@ -135,6 +136,8 @@ class IEngine {
   virtual void const_inj(int src, int dst, int kin, double f0) = 0;
   virtual void sync() = 0;
   virtual int kernel_launches() const = 0;
+  // JSON text of the launch-schedule autotuner's measurements and choices
+  virtual std::string plan_report() const = 0;
   // Per-kernel device time of nsteps RK4 steps with the dt already set,
   // measured with CUDA events recorded on the engine stream around every
   // launch: ms[k] = total milliseconds, cnt[k] = launches, for k = 0 pass A,

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -115,6 +116,7 @@ class EngineT final : public IEngine {
                      "memset plane");
       build_twiddles();
       set_kernel_attrs();
+      if (full) autotune();
       sync();
     } catch (...) {
       release();
@@ -575,6 +577,14 @@ class EngineT final : public IEngine {
                                                    planes_[dst_plane], gd_, r * r);
     post("k_coarsen");
   }
+  void refine_from(IEngine* coarse, int coarse_plane, int dst_plane) override {
+    if (coarse->precision() != precision() || coarse->n() >= n_)
+      throw Error(kEINVAL, "refine: coarser grid of the same precision");
+    const double r = (double)n_ / (double)coarse->n();
+    k_refine<T><<<elem_blocks(S_), 256, 0, st_>>>(static_cast<const cpx<T>*>(coarse->plane_ptr(coarse_plane)),
+                                                  coarse->n(), planes_[dst_plane], gd_, r * r);
+    post("k_refine");
+  }
   void closure_targets(IEngine* fine, float* d_y) override {
     // tau = P_c([.,.]_fine) - [.,.]_coarse for both brackets, in physical space
     fine->brackets();
@@ -860,17 +870,22 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       constexpr int NR = PassNT<T, N>::value;
       using C = Cfg<T, N, NR>;
+      bool persistent = false;
       if constexpr (kPipeB<T, N>) {
-        // persistent: about as many CTAs as fit on the device at once
-        constexpr int EP = PipeB<N>::E;
-        static_assert(EP == PassAE<T, N>::value || EP == Cfg<T, N>::E, "pass B radix has a twiddle table");
-        const tw_t<T>* twp = EP == PassAE<T, N>::value ? tw_a_ : tw_;
-        const int per_run = std::max(1, std::min(N / 2, (pipeb_ctas_ + nb - 1) / nb));
-        auto k = k_passB_pipe<N, CFL>;
-        k<<<dim3(per_run, nb), PipeB<N>::THREADS, PipeB<N>::smem(gd_.M), st_>>>(tf, pb, kxo, gd_, inv4, twp,
-                                                                                  enc_base_, batch());
-        post("k_passB_pipe");
-      } else {
+        if (passb_mode_ == 1) {
+          // persistent: the autotuned CTA count (about as many as fit at once)
+          persistent = true;
+          constexpr int EP = PipeB<N>::E;
+          static_assert(EP == PassAE<T, N>::value || EP == Cfg<T, N>::E, "pass B radix has a twiddle table");
+          const tw_t<T>* twp = EP == PassAE<T, N>::value ? tw_a_ : tw_;
+          const int per_run = std::max(1, std::min(N / 2, (pipeb_grid_ + nb - 1) / nb));
+          auto k = k_passB_pipe<N, CFL>;
+          k<<<dim3(per_run, nb), PipeB<N>::THREADS, PipeB<N>::smem(gd_.M), st_>>>(tf, pb, kxo, gd_, inv4, twp,
+                                                                                    enc_base_, batch());
+          post("k_passB_pipe");
+        }
+      }
+      if (!persistent) {  // one CTA (group) per row pair; the only form below n = 2048
         auto k = k_passB<T, N, CFL>;
         const dim3 grid((N / NR + C::G - 1) / C::G, nb);
         k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
@@ -926,6 +941,79 @@ class EngineT final : public IEngine {
     });
   }
 
+  // Launch-schedule autotuner, run once when a full engine is created: the
+  // variants of pass B that compute bit-identical results (one CTA per row
+  // pair; persistent cp.async-staged CTAs, as many as are resident or half
+  // of that) are timed with CUDA events on this engine's own buffers (3
+  // launches after 2 untimed ones) and the fastest is kept.  The transform
+  // radices, which change the rounding, are fixed per n.
+  void autotune() {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      if constexpr (kPipeB<T, N>) {
+        const int saved = launches_;
+        cuda_check(cudaMemsetAsync(tf_, 0, sizeof(cpx<T>) * 6 * (size_t)gd_.M * n_ * nb_, st_), "memset");
+        int sms = 0;
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
+        struct Cand {
+          int mode, grid;
+        };
+        std::vector<Cand> cands = {{0, 0}, {1, pipeb_ctas_}};
+        if (pipeb_ctas_ >= 2 * sms) cands.push_back({1, pipeb_ctas_ / 2});
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+        cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+        float best = 0.f;
+        Cand pick = cands[0];
+        tune_.clear();
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+          passb_mode_ = cands[ci].mode;
+          pipeb_grid_ = cands[ci].grid;
+          for (int i = 0; i < 2; ++i) launch_passB<false>(gd_.M, tf_, pb_, nb_);
+          cuda_check(cudaEventRecord(e0, st_), "cudaEventRecord");
+          for (int i = 0; i < 3; ++i) launch_passB<false>(gd_.M, tf_, pb_, nb_);
+          cuda_check(cudaEventRecord(e1, st_), "cudaEventRecord");
+          cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+          float ms = 0.f;
+          cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+          const float us = 1e3f * ms / 3.f;
+          tune_.push_back({cands[ci].mode, cands[ci].grid, us});
+          if (ci == 0 || us < best) {
+            best = us;
+            pick = cands[ci];
+          }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        // R2D3C_PASSB=per_row_pair|persistent overrides the measured choice
+        if (const char* force = std::getenv("R2D3C_PASSB")) {
+          if (std::strcmp(force, "per_row_pair") == 0) pick = cands[0];
+          else if (std::strcmp(force, "persistent") == 0) pick = cands[1];
+          else throw Error(kEINVAL, "R2D3C_PASSB must be per_row_pair or persistent");
+        }
+        passb_mode_ = pick.mode;
+        pipeb_grid_ = pick.grid;
+        launches_ = saved;
+      }
+    });
+  }
+
+ public:
+  std::string plan_report() const override {
+    std::string r = "{\"pass_b\": [";
+    for (size_t i = 0; i < tune_.size(); ++i) {
+      char b[160];
+      snprintf(b, sizeof b, "%s{\"variant\": \"%s\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
+               tune_[i].mode ? "persistent" : "per_row_pair", tune_[i].grid, (double)tune_[i].us);
+      r += b;
+    }
+    char b[160];
+    snprintf(b, sizeof b, "], \"chosen\": \"%s\", \"ctas\": %d}", passb_mode_ ? "persistent" : "per_row_pair",
+             passb_mode_ ? pipeb_grid_ : 0);
+    return r + b;
+  }
+
+ private:
   void build_twiddles() {
     std::vector<double> c(n_), s(n_);
     host_unit_roots(n_, c.data(), s.data());
@@ -951,6 +1039,13 @@ class EngineT final : public IEngine {
   std::function<void(cudaStream_t)> hook_;
   unsigned long long hook_id_ = 0;
   int pipeb_ctas_ = 0;  // resident CTAs of the pipelined pass B (whole device)
+  int passb_mode_ = 0;  // 0: one CTA per row pair, 1: persistent (autotuned)
+  int pipeb_grid_ = 0;  // CTAs of the persistent pass B (autotuned)
+  struct TuneRec {
+    int mode, grid;
+    float us;
+  };
+  std::vector<TuneRec> tune_;
   cpx<T>* pbase_[P_COUNT] = {};
   double* scal_base_ = nullptr;
   unsigned long long* enc_base_ = nullptr;

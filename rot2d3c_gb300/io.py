@@ -192,3 +192,62 @@ def append_time_line(path: str, tag: str, time: float) -> None:
     """time_spec.txt (A4,F12.6) or time_field.txt (A3,F12.6)."""
     with open(path, "a") as f:
         f.write(tag + fortran_f(time, 12, 6) + "\n")
+
+
+# ---------------------------------------------------------------------------
+# Time averages of the outputs (python_scripts/SpectraAvg.py, FluxesAvg.py)
+# ---------------------------------------------------------------------------
+def _indexed(odir: str, head: str, start: int):
+    """Files head.NNNN.txt of odir with NNNN >= start, in index order."""
+    out = []
+    for name in sorted(os.listdir(odir)):
+        if name.startswith(head + ".") and name.endswith(".txt"):
+            num = name[len(head) + 1:-4]
+            if num.isdigit() and int(num) >= start:
+                out.append(os.path.join(odir, name))
+    return out
+
+
+def _loadtxt(path: str) -> np.ndarray:
+    return np.loadtxt(path, ndmin=2)
+
+
+def mean_injection(run_dir: str, start: int, iflow: int):
+    """Mean total energy and enstrophy injection from energy_bal.txt and
+    enstrophy_bal.txt rows start.. (FluxesAvg.py:33-48): random forcing
+    (iflow 3) halves the recorded injections."""
+    e = _loadtxt(os.path.join(run_dir, "energy_bal.txt"))
+    z = _loadtxt(os.path.join(run_dir, "enstrophy_bal.txt"))
+    inj, injz, injenst = e[:, 3], e[:, 4], z[:, 2]
+    if iflow == 3:
+        inj, injz, injenst = inj / 2.0, injz / 2.0, injenst / 2.0
+    return float(np.mean(inj[start:] + injz[start:])), float(np.mean(injenst[start:]))
+
+
+def average_spectra(odir: str, start: int):
+    """Mean (E_2D, E_z) over spectrum.NNNN.txt with NNNN >= start
+    (SpectraAvg.py:35-60): each file weighted 1/number of files."""
+    files = _indexed(odir, "spectrum", start)
+    if not files:
+        raise ValueError(f"no spectrum files with index >= {start} in {odir}")
+    e2d = ez = None
+    for f in files:
+        d = _loadtxt(f)
+        a, b = d[:, 0] / float(len(files)), d[:, 1] / float(len(files))
+        e2d = a if e2d is None else e2d + a
+        ez = b if ez is None else ez + b
+    return e2d, ez
+
+
+def average_fluxes(odir: str, start: int, injtot: float = 1.0, injenst: float = 1.0):
+    """Mean (enstrophy flux / injenst, 2-D energy flux / injtot, vz energy
+    flux / injtot) over fluxes.NNNN.txt with NNNN >= start (FluxesAvg.py:67-95)."""
+    files = _indexed(odir, "fluxes", start)
+    if not files:
+        raise ValueError(f"no fluxes files with index >= {start} in {odir}")
+    acc = None
+    for f in files:
+        d = _loadtxt(f)
+        t = np.stack([d[:, 0] / injenst, d[:, 1] / injtot, d[:, 2] / injtot]) / float(len(files))
+        acc = t if acc is None else acc + t
+    return acc[0], acc[1], acc[2]

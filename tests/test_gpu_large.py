@@ -82,3 +82,31 @@ def test_fp32_vs_fp64_at_8192_spectra(gpu):
     assert rel_l2(b32, b64) < 2e-5
     live = ek64 > 1e-12 * ek64.max()
     assert np.max(np.abs(ek32[live] - ek64[live]) / ek64[live]) < 1e-3
+
+
+def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch):
+    """The plan autotuner times the pass-B launch schedules at context
+    creation; both schedules give bit-identical steps, so the choice never
+    changes results."""
+    n = 4096
+    cp, ps, vz, fp, fz = _case(n, 11)
+    c = gpu.Context(cp, 1)
+    rep = c.plan_report()
+    assert {r["variant"] for r in rep["pass_b"]} == {"per_row_pair", "persistent"}
+    assert all(r["us"] > 0 for r in rep["pass_b"]) and rep["chosen"] in ("per_row_pair", "persistent")
+    c.destroy()
+    out = []
+    for mode in ("per_row_pair", "persistent"):
+        monkeypatch.setenv("R2D3C_PASSB", mode)
+        c = gpu.Context(cp, 1)
+        assert c.plan_report()["chosen"] == mode
+        c.set_state(ps, vz)
+        c.set_forcing(fp, fz)
+        c.set_time(0.0)
+        c.advance(2, gpu.DT_CFL, 0.5)
+        out.append(c.get_state())
+        c.destroy()
+    for u, v in zip(out[0], out[1]):
+        np.testing.assert_array_equal(u, v)
+    small = gpu.Context(params(64, iflow=0)[1], 1)
+    assert small.plan_report() == {"pass_b": [], "chosen": "per_row_pair", "ctas": 0}

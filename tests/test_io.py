@@ -76,3 +76,35 @@ def test_fluxes_are_running_sums(tmp_path):
     np.testing.assert_allclose(t, np.c_[f0, f1, f2])
     np.testing.assert_allclose(x, np.c_[np.cumsum(f0), np.cumsum(f1), np.cumsum(f2)])
     assert len(open(tmp_path / "fluxes.0001.txt").readline()) == 3 * 24 + 1
+
+
+def test_time_averages_of_spectra_and_fluxes(tmp_path):
+    """average_spectra / average_fluxes / mean_injection (the reference's
+    SpectraAvg.py, FluxesAvg.py) over files written by our own writers."""
+    from rot2d3c_gb300 import io
+    rng = np.random.default_rng(3)
+    nb = 9
+    spec, flx = [], []
+    for i in range(1, 6):
+        ek, ezk = rng.random(nb), rng.random(nb)
+        f0, f1, f2 = rng.standard_normal(nb), rng.standard_normal(nb), rng.standard_normal(nb)
+        ext = f"{i:04d}"
+        io.write_spectrum(str(tmp_path), ext, ek, ezk)
+        io.write_transfers(str(tmp_path), ext, f0, f1, f2)
+        if i >= 3:
+            spec.append((ek, ezk))
+            flx.append((np.cumsum(f0), np.cumsum(f1), np.cumsum(f2)))
+    e2d, ez = io.average_spectra(str(tmp_path), 3)
+    np.testing.assert_allclose(e2d, np.mean([s[0] for s in spec], axis=0), rtol=1e-13)
+    np.testing.assert_allclose(ez, np.mean([s[1] for s in spec], axis=0), rtol=1e-13)
+    rows = np.column_stack([np.linspace(0, 1, 8)] + [rng.random(8) for _ in range(11)])
+    np.savetxt(tmp_path / "energy_bal.txt", rows)
+    zrows = np.column_stack([np.linspace(0, 1, 8)] + [rng.random(8) for _ in range(4)])
+    np.savetxt(tmp_path / "enstrophy_bal.txt", zrows)
+    inj, injz = io.mean_injection(str(tmp_path), 2, 3)
+    assert inj == pytest.approx(np.mean(rows[2:, 3] + rows[2:, 4]) / 2)
+    assert injz == pytest.approx(np.mean(zrows[2:, 2]) / 2)
+    z, a, b = io.average_fluxes(str(tmp_path), 3, injtot=inj, injenst=injz)
+    np.testing.assert_allclose(z, np.mean([f[0] for f in flx], axis=0) / injz, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(a, np.mean([f[1] for f in flx], axis=0) / inj, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(b, np.mean([f[2] for f in flx], axis=0) / inj, rtol=1e-12, atol=1e-14)
