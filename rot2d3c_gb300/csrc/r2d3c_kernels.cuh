@@ -302,19 +302,23 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
   int kyi[C::E];
 #pragma unroll
   for (int q = 0; q < C::E; ++q) kyi[q] = ky_of(lane + q * C::TPF, N);
-  cpx<T> s[NT][C::E], v[NT][C::E];
+  // FP32 keeps the source column pair in registers across its fields; FP64
+  // (registers full) re-reads it for every field, from L2
+  constexpr bool KEEP = sizeof(T) == 4;
+  cpx<T> s[KEEP ? NT : 1][KEEP ? C::E : 1], v[NT][C::E];
+  auto src_at = [&](const cpx<T>* sp, int t, int q) -> cpx<T> {
+    const int col = kx0 + t, ky = kyi[q];
+    const bool in = col < gd.M && (ky <= gd.L && -ky <= gd.L) && col * col + ky * ky <= gd.kmaxi;
+    return in ? sp[(size_t)col * N + lane + q * C::TPF] : czero<T>();
+  };
 #pragma unroll 1
   for (int src = 0; src < 2; ++src) {  // psi for fields 0-3, vz for fields 4-5
     const cpx<T>* sp = src == 0 ? ps : vz;
+    if constexpr (KEEP) {
 #pragma unroll
-    for (int t = 0; t < NT; ++t) {
-      const int col = kx0 + t;
+      for (int t = 0; t < NT; ++t)
 #pragma unroll
-      for (int q = 0; q < C::E; ++q) {
-        const int ky = kyi[q];
-        const bool in = col < gd.M && (ky <= gd.L && -ky <= gd.L) && col * col + ky * ky <= gd.kmaxi;
-        s[t][q] = in ? sp[(size_t)col * N + lane + q * C::TPF] : czero<T>();
-      }
+        for (int q = 0; q < C::E; ++q) s[t][q] = src_at(sp, t, q);
     }
 #pragma unroll 1
     for (int f = src * 4; f < (src == 0 ? 4 : 6); ++f) {
@@ -325,7 +329,9 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
         for (int q = 0; q < C::E; ++q) {
           // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
           const T k = (f & 1) ? (T)kyi[q] : (T)col;
-          cpx<T> x = s[t][q];
+          cpx<T> x;
+          if constexpr (KEEP) x = s[t][q];
+          else x = src_at(sp, t, q);
           if (f == 2 || f == 3) {
             const T m = -(T)(col * col + kyi[q] * kyi[q]);  // laplak2: -ka2*a
             x = mkc<T>(m * x.x, m * x.y);
