@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <random>
@@ -197,6 +198,263 @@ k_conv(const bf16* __restrict__ in, const bf16* __restrict__ w, const float* __r
 }
 
 // ---------------------------------------------------------------------------
+// The same convolution on the 5th-generation tensor cores (tcgen05), for
+// W % 128 == 0.  A CTA of 128 threads owns 128 consecutive pixels of one
+// image row per tile (persistent over tiles).  Shared memory holds, in the
+// canonical no-swizzle K-major UMMA layout (core matrices of 8 rows x 16 bytes):
+//   halo  unit (r, c, p) = 16 bytes = channels 8c..8c+7 of pixel p of halo
+//         row r (r = dy, p = 0..129 <-> x0-1 .. x0+128, periodic), at
+//         ((r*NCH + c)*130 + p)*16: the A operand of tap (dy, dx), channel
+//         chunks c, c+1 is the descriptor starting at unit (dy, c, dx) with
+//         leading (K) byte offset 130*16 and stride (M) byte offset 128 --
+//         the shifted window needs no copy;
+//   weights unit (kc, n) = k = 8kc..8kc+7 of output channel n, at
+//         (kc*COUT + n)*16 (B operand, K-major: LBO = COUT*16, SBO = 128).
+// One elected thread issues the 9 * CIN/16 MMAs (M = 128, N = COUT, K = 16,
+// bf16 x bf16 -> f32) into a 32-column TMEM accumulator and commits them to
+// an mbarrier; the 4 warps then read their 32 TMEM lanes (one pixel per
+// thread, COUT columns) with tcgen05.ld for the epilogue.  Every wait is
+// bounded: a wait that runs out sets *err, waits once more (bounded) for the
+// MMAs in flight, frees the TMEM and ends the kernel.
+// ---------------------------------------------------------------------------
+constexpr int kTcPix = 128;          // pixels per tile (M)
+constexpr int kTcThreads = 128;
+constexpr unsigned kTcWaitLimit = 1u << 24;  // mbarrier polls before giving up
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor, no swizzle, K-major (version 1 for sm_100+)
+__device__ __forceinline__ unsigned long long umma_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
+  unsigned long long d = (unsigned long long)((saddr >> 4) & 0x3FFFu);
+  d |= (unsigned long long)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (unsigned long long)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= 1ull << 46;
+  return d;
+}
+// instruction descriptor of kind::f16: D f32, A and B bf16, both K-major
+__host__ __device__ constexpr unsigned umma_idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
+  for (unsigned i = 0; i < kTcWaitLimit; ++i) {
+    if (mbar_try_wait(addr, parity)) return true;
+    if (i > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&r)[N]);
+template <>
+__device__ __forceinline__ void tmem_ld32<32>(unsigned taddr, unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+template <>
+__device__ __forceinline__ void tmem_ld32<16>(unsigned taddr, unsigned (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tc_cp16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void tc_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void tc_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory");
+}
+
+template <int CIN, int COUT>
+struct TcConv {
+  static constexpr int NCH = CIN / 8;
+  static constexpr int HALO_UNITS = 3 * NCH * (kTcPix + 2);
+  static constexpr int W_UNITS = 9 * CIN * COUT / 8;
+  // output staging of one tile: y [128][COUT] f32 and a [128][COUT] bf16,
+  // 16-byte chunks XOR-swizzled within each pixel row
+  static constexpr int Y_UNITS = kTcPix * COUT / 4, A_UNITS = kTcPix * COUT / 8;
+  // two halo buffers (the next tile's is copied while this one's runs), the
+  // weights, the output staging, the mbarrier and the TMEM address
+  static constexpr size_t SMEM = (size_t)(2 * HALO_UNITS + W_UNITS + Y_UNITS + A_UNITS) * 16 + 64;
+};
+
+// halo of tile t into buffer dst (one cp.async commit group; empty when
+// t >= ntiles)
+template <int CIN>
+__device__ __forceinline__ void tc_stage_halo(uint4* dst, const bf16* __restrict__ in, int t, int ntiles, int H,
+                                              int W) {
+  constexpr int NCH = CIN / 8, HP = kTcPix + 2;
+  if (t < ntiles) {
+    const int tiles_x = W / kTcPix;
+    const int b = t / (tiles_x * H), gy = (t / tiles_x) % H, x0 = (t % tiles_x) * kTcPix;
+    for (int i = threadIdx.x; i < 3 * NCH * HP; i += kTcThreads) {
+      const int c = i % NCH, p = (i / NCH) % HP, r = i / (NCH * HP);
+      int sy = gy + r - 1, sx = x0 + p - 1;
+      sy += sy < 0 ? H : (sy >= H ? -H : 0);
+      sx += sx < 0 ? W : (sx >= W ? -W : 0);
+      tc_cp16(dst + (r * NCH + c) * HP + p, in + (((size_t)b * H + sy) * W + sx) * CIN + c * 8);
+    }
+  }
+  tc_commit();
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kTcThreads)
+k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float* __restrict__ bias, int H, int W,
+          int ntiles, float* __restrict__ y, bf16* __restrict__ a, int act, int cout_store, int* __restrict__ err) {
+  using TC = TcConv<CIN, COUT>;
+  constexpr int NCH = TC::NCH, HP = kTcPix + 2;
+  constexpr unsigned IDESC = umma_idesc_bf16(kTcPix, COUT);
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  uint4* s_halo = reinterpret_cast<uint4*>(tc_smem);  // two buffers
+  uint4* s_w = s_halo + 2 * TC::HALO_UNITS;
+  uint4* s_y = s_w + TC::W_UNITS;
+  uint4* s_a = s_y + TC::Y_UNITS;
+  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_a + TC::A_UNITS);
+  unsigned* s_tmem = reinterpret_cast<unsigned*>(s_bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // weights, already in the K-major UMMA layout: unit (kc, n) = k 8kc..8kc+7 of column n
+  for (int i = tid; i < TC::W_UNITS; i += kTcThreads) tc_cp16(s_w + i, wt + (size_t)i * 8);
+  tc_commit();
+  int t = blockIdx.x;
+  tc_stage_halo<CIN>(s_halo, in, t, ntiles, H, W);
+  const unsigned bar = smem_u32(s_bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(smem_u32(s_tmem))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const unsigned tmem = *s_tmem;
+  const int tiles_x = W / kTcPix;
+  unsigned phase = 0;
+  for (int it = 0; t < ntiles; t += gridDim.x, ++it) {
+    uint4* cur = s_halo + (it & 1) * TC::HALO_UNITS;
+    // the next tile's halo into the other buffer (its last reader, the
+    // previous tile's MMAs, has completed)
+    tc_stage_halo<CIN>(s_halo + ((it + 1) & 1) * TC::HALO_UNITS, in, t + gridDim.x, ntiles, H, W);
+    tc_wait<1>();  // weights and this tile's halo landed
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // visible to the tensor cores
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const unsigned hb = smem_u32(cur), wb = smem_u32(s_w);
+#pragma unroll
+      for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+        for (int kk = 0; kk < CIN / 16; ++kk) {
+          const unsigned long long ad = umma_desc(hb + (unsigned)(((dy * NCH + 2 * kk) * HP + dx) * 16), HP * 16, 128);
+          const int kc = (tap * CIN + 16 * kk) / 8;
+          const unsigned long long bd = umma_desc(wb + (unsigned)(kc * COUT * 16), COUT * 16, 128);
+          const unsigned accum = (tap | kk) ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(IDESC), "r"(accum)
+              : "memory");
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                   : "memory");
+    }
+    const bool done = mbar_wait_bounded(bar, phase);
+    if (__syncthreads_or(!done)) {  // the same decision in every thread
+      if (tid == 0) atomicExch(err, 1);
+      mbar_wait_bounded(bar, phase);  // one more bounded wait for the MMAs in flight
+      break;
+    }
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    unsigned r[COUT];
+    tmem_ld32<COUT>(tmem + ((unsigned)(warp * 32) << 16), r);
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    // epilogue: pixel m = 32*warp + lane of the tile, COUT accumulators
+    const int b = t / (tiles_x * H), gy = (t / tiles_x) % H, x0 = (t % tiles_x) * kTcPix;
+    const size_t pix0 = ((size_t)b * H + gy) * W + x0;  // the tile's pixels are contiguous
+    const int m = warp * 32 + lane;
+    float v[COUT];
+#pragma unroll
+    for (int co = 0; co < COUT; ++co) v[co] = __uint_as_float(r[co]) + (bias ? __ldg(bias + co) : 0.f);
+    if (y && cout_store < COUT) {
+      // the network output (2 channels): 8 bytes per pixel straight from registers
+#pragma unroll
+      for (int co = 0; co < COUT; co += 2)
+        if (co < cout_store) *reinterpret_cast<float2*>(y + (pix0 + m) * cout_store + co) = make_float2(v[co], v[co + 1]);
+    }
+    // full rows go through the swizzled staging so that the global stores of
+    // the tile are contiguous 16-byte chunks
+    constexpr int YC = COUT / 4, AC = COUT / 8;  // 16-byte chunks per pixel row
+    if (y && cout_store == COUT) {
+#pragma unroll
+      for (int c = 0; c < YC; ++c)
+        s_y[m * YC + (c ^ (m % YC))] = make_uint4(__float_as_uint(v[4 * c]), __float_as_uint(v[4 * c + 1]),
+                                                  __float_as_uint(v[4 * c + 2]), __float_as_uint(v[4 * c + 3]));
+    }
+    if (a) {
+#pragma unroll
+      for (int c = 0; c < AC; ++c) {
+        unsigned u[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float p0 = v[8 * c + 2 * e], p1 = v[8 * c + 2 * e + 1];
+          u[e] = pack_bf16(__float2bfloat16_rn(act ? gelu(p0) : p0), __float2bfloat16_rn(act ? gelu(p1) : p1));
+        }
+        s_a[m * AC + (c ^ ((m / (8 / AC)) % AC))] = make_uint4(u[0], u[1], u[2], u[3]);
+      }
+    }
+    __syncthreads();  // staging complete; TMEM read before the next tile's MMAs
+    if (y && cout_store == COUT) {
+      uint4* gy4 = reinterpret_cast<uint4*>(y + pix0 * COUT);
+      for (int q = tid; q < TC::Y_UNITS; q += kTcThreads) {
+        const int mm = q / YC, c = q % YC;
+        gy4[q] = s_y[mm * YC + (c ^ (mm % YC))];
+      }
+    }
+    if (a) {
+      uint4* ga4 = reinterpret_cast<uint4*>(a + pix0 * COUT);
+      for (int q = tid; q < TC::A_UNITS; q += kTcThreads) {
+        const int mm = q / AC, c = q % AC;
+        ga4[q] = s_a[mm * AC + (c ^ ((mm / (8 / AC)) % AC))];
+      }
+    }
+    // the staging is rewritten only after the next tile's barriers
+  }
+  tc_wait<0>();  // no copy outlives the CTA
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(tmem) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
 // dW[k][co] and db[co] partials: CTA c accumulates over pixel tiles c,
 // c + grid, ...  in: [B][H][W][CIN] bf16, dy: [B][H][W][COUT] bf16;
 // part: [grid][9*CIN*COUT + COUT] (weights, then bias).  The GEMM is
@@ -351,14 +609,21 @@ __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float
 }
 
 // master weights [9][cin][cout] (unpadded) -> wf [9*CINP][COUTP], wb [9*COUTP][CINP]
+// and the same two matrices in the K-major UMMA layout of the tensor-core
+// convolution: element (k, n) of a K x N matrix at ((k/8)*N + n)*8 + k%8.
 __global__ void k_pack_weights(const float* __restrict__ wm, int cin, int cout, int cinp, int coutp,
-                               bf16* __restrict__ wf, bf16* __restrict__ wb) {
+                               bf16* __restrict__ wf, bf16* __restrict__ wb, bf16* __restrict__ wtf,
+                               bf16* __restrict__ wtb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 9 * cinp * coutp) return;
   const int co = i % coutp, ci = (i / coutp) % cinp, tap = i / (coutp * cinp);
   const float v = (ci < cin && co < cout) ? wm[((size_t)tap * cin + ci) * cout + co] : 0.f;
-  wf[((size_t)tap * cinp + ci) * coutp + co] = __float2bfloat16_rn(v);
-  wb[((size_t)(8 - tap) * coutp + co) * cinp + ci] = __float2bfloat16_rn(v);
+  const bf16 h = __float2bfloat16_rn(v);
+  const int kf = tap * cinp + ci, kb = (8 - tap) * coutp + co;
+  wf[(size_t)kf * coutp + co] = h;
+  wb[(size_t)kb * cinp + ci] = h;
+  wtf[((size_t)(kf >> 3) * coutp + co) * 8 + (kf & 7)] = h;
+  wtb[((size_t)(kb >> 3) * cinp + ci) * 8 + (kb & 7)] = h;
 }
 
 // padded weight gradient [9][cinp][coutp] -> parameter layout [9][cin][cout];
@@ -421,6 +686,37 @@ void conv_launch(const bf16* in, const bf16* w, const float* b, int B, int H, in
 }
 
 template <int CIN, int COUT>
+void conv_tc_launch(const bf16* in, const bf16* w, const float* b, int B, int H, int W, float* y, bf16* a, int act,
+                    int cout_store, int ctas, int* err, cudaStream_t st) {
+  const int tiles = B * H * (W / kTcPix);
+  k_conv_tc<CIN, COUT><<<std::min(tiles, ctas), kTcThreads, TcConv<CIN, COUT>::SMEM, st>>>(
+      in, w, b, H, W, tiles, y, a, act, cout_store, err);
+}
+template <int CIN, int COUT>
+int resident_tc_ctas() {
+  cuda_check(cudaFuncSetAttribute(k_conv_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)TcConv<CIN, COUT>::SMEM),
+             "cudaFuncSetAttribute(max dynamic smem)");
+  // the whole unified L1/shared array as shared memory, so that several
+  // CTAs (and their copy pipelines) share each SM
+  cuda_check(cudaFuncSetAttribute(k_conv_tc<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared),
+             "cudaFuncSetAttribute(carveout)");
+  int dev = 0, sms = 0, per_sm = 0, smem_sm = 0, reserved = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc<CIN, COUT>, kTcThreads,
+                                                           TcConv<CIN, COUT>::SMEM),
+             "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+  // the shared-memory bound itself (with the carveout at its maximum)
+  cuda_check(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev),
+             "cudaDeviceGetAttribute");
+  cuda_check(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev), "cudaDeviceGetAttribute");
+  const int by_smem = smem_sm / (int)(TcConv<CIN, COUT>::SMEM + reserved);
+  return std::max(1, std::max(per_sm, std::min(by_smem, 8))) * sms;
+}
+
+template <int CIN, int COUT>
 void wgrad_launch(const bf16* in, const bf16* dy, int B, int H, int W, float* part, int nparts, cudaStream_t st) {
   const int tiles = B * (H / TH) * (W / TW);
   k_conv_wgrad<CIN, COUT><<<nparts, kThreads, 0, st>>>(in, dy, H, W, tiles, part);
@@ -432,12 +728,17 @@ struct r2d3c_cnn {
   int H = 0, W = 0, Bmax = 0;
   unsigned long long serial = 0;  // unique per network created in this process
   int ctas[3] = {};               // resident CTAs of k_conv<16,32>, <32,32>, <32,16>
+  int tc_ctas[3] = {};            // and of k_conv_tc
+  bool use_tc = false;            // tcgen05 convolutions (W % 128 == 0)
+  int* err = nullptr;             // set by a device wait that gave up
   cudaStream_t st = nullptr;
   Layer L[kLayers];
   size_t nparam = 0;
   float *wm = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;  // master params, grads, Adam moments
   bf16* wf[kLayers] = {};
   bf16* wb[kLayers] = {};
+  bf16* wtf[kLayers] = {};  // forward / backward-data weights in the UMMA layout
+  bf16* wtb[kLayers] = {};
   bf16* act[kLayers + 1] = {};   // act[0] = bf16 input (16 ch), act[l+1] = layer l output (bf16)
   float* pre[kLayers] = {};      // pre-activations y (f32), last = network output (2 ch)
   bf16 *dA = nullptr, *dY = nullptr;
@@ -459,12 +760,30 @@ struct r2d3c_cnn {
     if (st) cudaStreamDestroy(st);
   }
 
+  // a bounded device wait that gave up (tcgen05 convolutions) -> R2D3C_ETIMEOUT
+  void check_err() {
+    int h = 0;
+    cuda_check(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H error flag");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    if (h) {
+      cuda_check(cudaMemsetAsync(err, 0, sizeof(int), st), "memset");
+      throw Error(kETIMEOUT, "a tensor-core convolution wait gave up");
+    }
+  }
   void conv(int l, const bf16* in, const bf16* w, int B, float* y, bf16* a, int act_on, bool bias, bool back) {
     const float* b = bias ? wm + L[l].boff : nullptr;
     // forward shapes (CINP, COUTP) or backward-data shapes (COUTP, CINP)
     const int ci = back ? L[l].coutp : L[l].cinp, co = back ? L[l].cinp : L[l].coutp;
     const int store = back ? co : (l == kLayers - 1 ? L[l].cout : co);
-    if (ci == 16 && co == 32) conv_launch<16, 32>(in, w, b, B, H, W, y, a, act_on, store, ctas[0], st);
+    if (use_tc) {
+      const bf16* wt = back ? wtb[l] : wtf[l];  // the same matrix as w, UMMA layout
+      if (ci == 16 && co == 32) conv_tc_launch<16, 32>(in, wt, b, B, H, W, y, a, act_on, store, tc_ctas[0], err, st);
+      else if (ci == 32 && co == 32)
+        conv_tc_launch<32, 32>(in, wt, b, B, H, W, y, a, act_on, store, tc_ctas[1], err, st);
+      else if (ci == 32 && co == 16)
+        conv_tc_launch<32, 16>(in, wt, b, B, H, W, y, a, act_on, store, tc_ctas[2], err, st);
+      else throw Error(kEINVAL, "unsupported conv shape");
+    } else if (ci == 16 && co == 32) conv_launch<16, 32>(in, w, b, B, H, W, y, a, act_on, store, ctas[0], st);
     else if (ci == 32 && co == 32) conv_launch<32, 32>(in, w, b, B, H, W, y, a, act_on, store, ctas[1], st);
     else if (ci == 32 && co == 16) conv_launch<32, 16>(in, w, b, B, H, W, y, a, act_on, store, ctas[2], st);
     else throw Error(kEINVAL, "unsupported conv shape");
@@ -532,7 +851,8 @@ struct r2d3c_cnn {
     for (int l = 0; l < kLayers; ++l) {
       const Layer& ly = L[l];
       const int c = 9 * ly.cinp * ly.coutp;
-      k_pack_weights<<<(c + 255) / 256, 256, 0, st>>>(wm + ly.woff, ly.cin, ly.cout, ly.cinp, ly.coutp, wf[l], wb[l]);
+      k_pack_weights<<<(c + 255) / 256, 256, 0, st>>>(wm + ly.woff, ly.cin, ly.cout, ly.cinp, ly.coutp, wf[l], wb[l],
+                                                      wtf[l], wtb[l]);
       cuda_check(cudaGetLastError(), "k_pack_weights");
     }
   }
@@ -564,6 +884,7 @@ void cnn_forward_on(r2d3c_cnn* c, const float* d_x, int batch, float* d_out, cud
   }
   c->st = own;
 }
+void cnn_check_err(r2d3c_cnn* c) { c->check_err(); }
 void cnn_shape(const r2d3c_cnn* c, int* H, int* W, int* max_batch, unsigned long long* serial) {
   *H = c->H;
   *W = c->W;
@@ -596,6 +917,17 @@ int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** out) {
     c->ctas[0] = resident_ctas(k_conv<16, 32>);
     c->ctas[1] = resident_ctas(k_conv<32, 32>);
     c->ctas[2] = resident_ctas(k_conv<32, 16>);
+    // tcgen05 convolutions where a tile of 128 pixels fits a row;
+    // R2D3C_CNN_CONV=mma selects the warp-level MMA kernels everywhere
+    const char* conv_env = std::getenv("R2D3C_CNN_CONV");
+    if (conv_env && std::strcmp(conv_env, "mma") != 0 && std::strcmp(conv_env, "tcgen05") != 0)
+      throw Error(kEINVAL, "R2D3C_CNN_CONV must be mma or tcgen05");
+    c->use_tc = W % kTcPix == 0 && !(conv_env && std::strcmp(conv_env, "mma") == 0);
+    if (c->use_tc) {
+      c->tc_ctas[0] = resident_tc_ctas<16, 32>();
+      c->tc_ctas[1] = resident_tc_ctas<32, 32>();
+      c->tc_ctas[2] = resident_tc_ctas<32, 16>();
+    }
     cuda_check(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate");
     size_t off = 0;
     for (int l = 0; l < kLayers; ++l) {
@@ -625,6 +957,8 @@ int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** out) {
     for (int l = 0; l < kLayers; ++l) {
       c->wf[l] = c->alloc<bf16>((size_t)9 * kCinPad[l] * kCoutPad[l]);
       c->wb[l] = c->alloc<bf16>((size_t)9 * kCinPad[l] * kCoutPad[l]);
+      c->wtf[l] = c->alloc<bf16>((size_t)9 * kCinPad[l] * kCoutPad[l]);
+      c->wtb[l] = c->alloc<bf16>((size_t)9 * kCinPad[l] * kCoutPad[l]);
       c->pre[l] = c->alloc<float>(npix * (l == kLayers - 1 ? kCout[l] : kCoutPad[l]));
     }
     c->act[0] = c->alloc<bf16>(npix * 16);
@@ -634,6 +968,8 @@ int r2d3c_cnn_create(int H, int W, int max_batch, int seed, r2d3c_cnn** out) {
     c->part = c->alloc<float>((size_t)(c->nparts + 1) * (9 * 32 * 32 + 32));
     c->lpart = c->alloc<float>(256);
     c->norm = c->alloc<float>(20);
+    c->err = c->alloc<int>(1);
+    cuda_check(cudaMemsetAsync(c->err, 0, sizeof(int), c->st), "memset");
     const float ident[20] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 1, 1};
     cuda_check(cudaMemcpyAsync(c->norm, ident, sizeof(ident), cudaMemcpyHostToDevice, c->st), "H2D");
     c->pack();
@@ -713,7 +1049,7 @@ int r2d3c_cnn_forward(r2d3c_cnn* c, const float* d_x, int batch, float* d_out) {
     k_denorm<<<512, 256, 0, c->st>>>(c->pre[kLayers - 1], (size_t)batch * c->H * c->W, c->norm + 16, c->norm + 18,
                                      d_out);
     cuda_check(cudaGetLastError(), "k_denorm");
-    cuda_check(cudaStreamSynchronize(c->st), "sync");
+    c->check_err();
   } catch (const Error& e) {
     return fail(e);
   }
@@ -727,6 +1063,7 @@ int r2d3c_cnn_gradients(r2d3c_cnn* c, const float* d_x, const float* d_y, int ba
     if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
     c->forward(d_x, batch);
     const double l = c->backward(d_y, batch);
+    c->check_err();
     if (loss) *loss = l;
     if (host_grad) {
       cuda_check(cudaMemcpyAsync(host_grad, c->grad, c->nparam * sizeof(float), cudaMemcpyDeviceToHost, c->st),
@@ -746,7 +1083,7 @@ int r2d3c_cnn_train_step(r2d3c_cnn* c, const float* d_x, const float* d_y, int b
     c->forward(d_x, batch);
     const double l = c->backward(d_y, batch);
     c->adam(lr);
-    cuda_check(cudaStreamSynchronize(c->st), "sync");
+    c->check_err();
     if (loss) *loss = l;
   } catch (const Error& e) {
     return fail(e);

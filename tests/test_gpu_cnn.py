@@ -18,7 +18,7 @@ def _layer_slices():
     return out
 
 
-@pytest.mark.parametrize("H,W,B", [(8, 16, 2), (16, 32, 1)])
+@pytest.mark.parametrize("H,W,B", [(8, 16, 2), (16, 32, 1), (8, 128, 2), (8, 256, 1)])
 def test_forward_and_gradients_match_reference(gpu, H, W, B):
     import torch
     from rot2d3c_gb300.closure import CNN
@@ -62,3 +62,27 @@ def test_training_lowers_the_loss(gpu):
     for _ in range(300):
         last = net.train_step(dx, dt, B, 3e-3)
     assert np.isfinite(last) and last < 0.1 * first
+
+
+def test_tensor_core_convolutions_match_the_warp_mma_ones(gpu, monkeypatch):
+    """W % 128 == 0 runs the tcgen05 convolutions (TMEM accumulators); the
+    same network with R2D3C_CNN_CONV=mma runs the warp-level MMA kernels:
+    outputs, loss and gradients agree to the accumulation-order level."""
+    import torch
+    from rot2d3c_gb300.closure import CNN
+    H, W, B = 16, 256, 2
+    rng = np.random.default_rng(5)
+    x = torch.from_numpy(rng.standard_normal((B, H, W, 8)).astype(np.float32)).cuda()
+    t = torch.from_numpy((0.1 * rng.standard_normal((B, H, W, 2))).astype(np.float32)).cuda()
+    res = []
+    for mode in ("tcgen05", "mma"):
+        monkeypatch.setenv("R2D3C_CNN_CONV", mode)
+        net = CNN(H, W, B, seed=9)
+        out = torch.empty((B, H, W, 2), dtype=torch.float32, device="cuda")
+        net.forward(x, B, out)
+        loss, g = net.gradients(x, t, B)
+        res.append((out.cpu().numpy(), loss, g))
+    (o1, l1, g1), (o2, l2, g2) = res
+    assert np.linalg.norm(o1 - o2) <= 1e-2 * np.linalg.norm(o2)
+    assert abs(l1 - l2) <= 1e-3 * l2
+    assert np.linalg.norm(g1 - g2) <= 1e-2 * np.linalg.norm(g2)
