@@ -341,8 +341,8 @@ def run_ensemble(args, torch):
 
 
 # ---------------------------------------------------------------- closure
-CLOSURE = dict(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=10, spinup=2000, train_steps=3000,
-               batch=32, lr=1e-3, les_steps=4000, cfl=0.5, seed=1)
+CLOSURE = dict(nf=2048, nc=256, omega=1.0, nu=2e-5, hnu=1.0, nsnap=1000, snap_every=20, spinup=10000,
+               train_steps=6000, batch=32, lr=5e-4, les_steps=4000, cfl=0.5, seed=1)
 
 
 def run_closure():

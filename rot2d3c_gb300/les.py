@@ -81,12 +81,12 @@ def coarse_forcing(fp, fz, nf, nc):
 
 def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=10, spinup=2000,
                    train_steps=3000, batch=32, lr=1e-3, les_steps=4000, cfl=0.5, seed=1,
-                   fallback_nn=4, spec_every=50):
+                   fallback_nn=4, spec_every=50, hnu=0.1):
     """Runs the three stages and returns a dict of timings and errors.
 
     nf, nc: DNS and LES grids; nu: viscosity of both (nn = 1); omega:
-    rotation rate; nsnap snapshots taken every snap_every DNS steps after
-    spinup steps; train_steps Adam steps of batch snapshots; les_steps coarse
+    rotation rate; hnu: large-scale (hypo)viscosity of all runs (mm = 2);
+    nsnap snapshots taken every snap_every DNS steps after spinup steps; train_steps Adam steps of batch snapshots; les_steps coarse
     CFL steps, whose second half is averaged for the spectra (one spectrum
     every spec_every steps).  The fallback run replaces the viscosity by a
     hyperviscosity of order fallback_nn with the damping rate 20 nu k_c^2
@@ -97,7 +97,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
     les_steps = max(spec_every, les_steps // spec_every * spec_every)
     t_all = time.perf_counter()
     ps, vz, fp, fz = _setup_run(nf, seed)
-    pf = make_params(n=nf, nu=nu, nuv=nu, hnu=0.1, hnuv=0.1, nn=1, mm=2, nnv=1, mmv=2, omega=omega, iflow=0,
+    pf = make_params(n=nf, nu=nu, nuv=nu, hnu=hnu, hnuv=hnu, nn=1, mm=2, nnv=1, mmv=2, omega=omega, iflow=0,
                      cfl=cfl)
     fine = Context(pf, FP32)
     fine.set_state(ps, vz)
@@ -105,7 +105,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
     fine.set_time(0.0)
     t_dns, _ = fine.advance(spinup, DT_CFL, cfl)
     # ---- 1. training data
-    pc = make_params(n=nc, nu=nu, nuv=nu, hnu=0.1, hnuv=0.1, nn=1, mm=2, nnv=1, mmv=2, omega=omega, iflow=0,
+    pc = make_params(n=nc, nu=nu, nuv=nu, hnu=hnu, hnuv=hnu, nn=1, mm=2, nnv=1, mmv=2, omega=omega, iflow=0,
                      cfl=cfl)
     coarse = Context(pc, FP32)
     X = torch.empty((nsnap, nc, nc, 8), dtype=torch.float32, device="cuda")
@@ -144,7 +144,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
     cfp, cfz = coarse_forcing(fp, fz, nf, nc)
     runs = {}
     for name, nn_, nuc in (("les", 1, nu), ("plain", 1, nu), ("fallback", fallback_nn, None)):
-        p = make_params(n=nc, nu=nu, nuv=nu, hnu=0.1, hnuv=0.1, nn=nn_, mm=2, nnv=nn_, mmv=2, omega=omega, iflow=0,
+        p = make_params(n=nc, nu=nu, nuv=nu, hnu=hnu, hnuv=hnu, nn=nn_, mm=2, nnv=nn_, mmv=2, omega=omega, iflow=0,
                         cfl=cfl)
         if nuc is None:  # hyperviscosity with the same damping rate at the coarse cutoff
             kc = nc / 3.0
@@ -231,5 +231,5 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
         "training": {"snapshots": nsnap, "steps": train_steps, "batch": batch, "data_s": t_data, "train_s": t_train,
                      "loss_first": losses[0], "loss_last": float(np.mean(losses[-20:])),
                      "val_loss": float(np.mean(val)) if val else None},
-        "omega": omega, "nu": nu, "total_s": time.perf_counter() - t_all,
+        "omega": omega, "nu": nu, "hnu": hnu, "total_s": time.perf_counter() - t_all,
     }
