@@ -100,6 +100,7 @@ struct r2d3c_ctx {
 namespace r2d3c {
 void cnn_forward_on(r2d3c_cnn* c, const float* d_x, int batch, float* d_out, cudaStream_t stream);
 void cnn_shape(const r2d3c_cnn* c, int* H, int* W, int* max_batch, unsigned long long* serial);
+void cnn_check_err(r2d3c_cnn* c);
 }  // namespace r2d3c
 
 struct r2d3c_plan {
@@ -1090,6 +1091,7 @@ int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mod
   if (time) *time = e->get_time();
   if (dt_last) *dt_last = e->get_dt();
   e->sync();
+  cnn_check_err(cnn);
   API_END
 }
 
