@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-steps", type=int, default=500)
     ap.add_argument("--no-closure", action="store_true")
+    ap.add_argument("--closure-small", action="store_true",
+                    help="closure leg on a small case (512^2 DNS, 128^2 LES, few steps): for profiling its kernels")
     return ap.parse_args()
 
 
@@ -345,20 +347,25 @@ CLOSURE = dict(nf=2048, nc=256, omega=1.0, nu=2e-5, hnu=1.0, nsnap=1000, snap_ev
                train_steps=6000, batch=32, lr=5e-4, les_steps=4000, cfl=0.5, seed=1)
 
 
-def run_closure():
+CLOSURE_SMALL = dict(CLOSURE, nf=512, nc=128, nu=2e-4, nsnap=64, snap_every=5, spinup=200, train_steps=40,
+                     les_steps=200, spec_every=20)
+
+
+def run_closure(small=False):
     """The learned-closure experiment (rot2d3c_gb300.les): FP32 DNS at 2048^2,
     filtered snapshots, CNN training, then the 256^2 LES with the network in
     the loop against the plain and hyperviscous coarse solvers and the
     filtered DNS over the same physical time.  The gain is the DNS's GPU
     seconds over the LES's for that time."""
     from rot2d3c_gb300.les import run_experiment
-    r = run_experiment(**CLOSURE)
+    cfg = CLOSURE_SMALL if small else CLOSURE
+    r = run_experiment(**cfg)
     tr = r["training"]
     return {"les_vs_dns_gain": r["les"]["gain"], "unit": "DNS GPU-s / LES GPU-s (same physical time)",
             "dns": r["dns"], "les": r["les"], "spectrum_error": r["spectrum_error"],
             "training": dict(tr, ms_per_step=1e3 * tr["train_s"] / tr["steps"],
                              samples_per_s=tr["steps"] * tr["batch"] / tr["train_s"]),
-            "config": dict(CLOSURE, network="6 x conv3x3 8-32-32-32-32-32-2, GELU, BF16 tensor-core MMA, FP32 master "
+            "config": dict(cfg, network="6 x conv3x3 8-32-32-32-32-32-2, GELU, BF16 tensor-core MMA, FP32 master "
                                            "weights, Adam; dataset and LES on GPU"),
             "total_s": r["total_s"]}
 
@@ -553,7 +560,7 @@ def main():
         cpu = cpu_baseline(n, ps, vz, fp, fz)
     closure = None
     if rank == 0 and world == 1 and not args.no_closure:
-        closure = run_closure()
+        closure = run_closure(args.closure_small)
 
     line = {"metric": METRIC, "value": v32, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": 1e3 * el32 / K, "higher_is_better": True, "scaling": "weak",
