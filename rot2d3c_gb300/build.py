@@ -1,9 +1,11 @@
-"""Build recipe of the CUDA library ``librot2d3c_gb300.so`` (sm_103a only).
+"""Build recipe of the CUDA library ``librot2d3c_gb300.so`` (sm_103a only)
+and of the main-program executable ``bin/rot2d3c_gpu`` linked against it.
 
-Three translation units (C-ABI, FP64 engine, FP32 engine) are compiled in
-parallel with nvcc and linked into one shared library next to this file.
-The build is incremental: nothing is recompiled when the library is newer
-than every source and header.
+The translation units (C-ABI, FP64 engine, FP32 engine, allocation-free
+transform, closure CNN) are compiled in parallel with nvcc and linked into
+one shared library next to this file; the C++ main program (``app/``) is
+compiled with the host C++ compiler.  The build is incremental: nothing is
+recompiled when the outputs are newer than every source and header.
 """
 from __future__ import annotations
 
@@ -17,6 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librot2d3c_gb300.so")
+APP_SRC = os.path.join(HERE, "app", "rot2d3c_gpu.cpp")
+APP = os.path.join(HERE, "bin", "rot2d3c_gpu")
 SOURCES = [
     "r2d3c_api.cu", "r2d3c_engine_f64.cu", "r2d3c_engine_f32.cu", "r2d3c_noalloc.cu", "r2d3c_cnn.cu",
 ]
@@ -38,10 +42,26 @@ def _deps():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(APP):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(f) <= t for f in _deps())
+    t = min(os.path.getmtime(LIB), os.path.getmtime(APP))
+    return all(os.path.getmtime(f) <= t for f in _deps() + [APP_SRC])
+
+
+def build_app() -> str:
+    """The main program, linked against the library (found next to bin/)."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no host C++ compiler for the main program")
+    os.makedirs(os.path.dirname(APP), exist_ok=True)
+    tmp = APP + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, APP_SRC, "-o", tmp, "-L", HERE, "-lrot2d3c_gb300",
+           "-Wl,-rpath,$ORIGIN/.."]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("main program build failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, APP)
+    return APP
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -74,8 +94,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)
+    build_app()
     if verbose:
-        print("built", LIB, file=sys.stderr)
+        print("built", LIB, "and", APP, file=sys.stderr)
     return LIB
 
 
