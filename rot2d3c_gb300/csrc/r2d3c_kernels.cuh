@@ -424,6 +424,23 @@ __device__ __forceinline__ void packed_pair(const cpx<T>* __restrict__ pa, const
 // pass B: per group NR rows; the two brackets in physical space and back to
 // mixed space
 // --------------------------------------------------------------------------
+// CFL maximum of |grad psi|^2 = x^2 + y^2 over a thread's values of
+// z1 = d_x psi + i d_y psi (CFL_condition, pseudospec2D_Rot2D3C.f90:867-874),
+// folded into the run's encoded maximum.  The squares are formed in the
+// compute type (an FP64 square per value would double the FP32 pass's time
+// on GB300's FP64 rate); the maximum is kept in FP64.
+template <typename T, int NT, int E>
+__device__ __forceinline__ void cfl_max_sq(const cpx<T> (&v)[NT][E], unsigned long long* enc) {
+  T m = (T)0;
+#pragma unroll
+  for (int t = 0; t < NT; ++t)
+#pragma unroll
+    for (int q = 0; q < E; ++q) m = max(m, v[t][q].x * v[t][q].x + v[t][q].y * v[t][q].y);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(enc, enc_ordered((double)m));
+}
+
 template <typename T, int N, bool CFL>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
@@ -458,19 +475,7 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
     for (int t = 0; t < NR; ++t) v[t][q] = z[t];
   }
   F::template run<+1>(v, lane, sm, tw);
-  if constexpr (CFL) {
-    double m = 0.0;
-#pragma unroll
-    for (int t = 0; t < NR; ++t)
-#pragma unroll
-      for (int q = 0; q < C::E; ++q) {
-        const double rx = (double)v[t][q].x, ry = (double)v[t][q].y;
-        m = fmax(m, rx * rx + ry * ry);
-      }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(cfl_enc, enc_ordered(m));
-  }
+  if constexpr (CFL) cfl_max_sq<T, NR, C::E>(v, cfl_enc);
   // each thread reads back only the positions it wrote: no barrier needed
   auto z1 = [&](int t, int q) -> cpx<T> {
     if constexpr (HOLD) return hold[t * N + lane + q * C::TPF];
@@ -695,19 +700,7 @@ k_passB_pipe(const float2* __restrict__ tf, float2* __restrict__ pb, int kxo, De
       }
       F::template run<+1>(v, lane, sm, tw);
       if (f == 0) {
-        if constexpr (CFL) {
-          double m = 0.0;
-#pragma unroll
-          for (int t = 0; t < NT; ++t)
-#pragma unroll
-            for (int q = 0; q < E; ++q) {
-              const double rx = (double)v[t][q].x, ry = (double)v[t][q].y;
-              m = fmax(m, rx * rx + ry * ry);
-            }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-          if ((threadIdx.x & 31) == 0) atomicMax(cfl_enc, enc_ordered(m));
-        }
+        if constexpr (CFL) cfl_max_sq<T, NT, E>(v, cfl_enc);
         // each thread reads back only the positions it wrote: no barrier needed
 #pragma unroll
         for (int t = 0; t < NT; ++t)
