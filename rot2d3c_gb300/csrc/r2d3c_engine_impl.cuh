@@ -929,6 +929,12 @@ class EngineT final : public IEngine {
         const size_t smp = PipeB<N>::smem(gd_.M);
         set_smem_attr(k_passB_pipe<N, true>, smp);
         set_smem_attr(k_passB_pipe<N, false>, smp);
+        // all of the unified L1/shared array as shared memory: as many
+        // persistent CTAs per SM as their shared memory allows
+        for (auto k : {k_passB_pipe<N, true>, k_passB_pipe<N, false>})
+          cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          (int)cudaSharedmemCarveoutMaxShared),
+                     "cudaFuncSetAttribute(carveout)");
         int per_sm = 0, sms = 0, dev = 0;
         cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_passB_pipe<N, true>,
                                                                  PipeB<N>::THREADS, smp),

@@ -600,7 +600,9 @@ struct PipeB {
   using F = BlockFFT<float, N, E, NT>;
   static constexpr int TPF = N / E;
   static constexpr int THREADS = G * TPF;
-  static constexpr int MINB = N >= 4096 ? 1 : 2;  // CTAs per SM (shared memory allows one at n = 4096)
+  // CTAs per SM the registers are sized for: 16 warps per SM at 128 registers
+  // (shared memory allows exactly one CTA at n = 4096)
+  static constexpr int MINB = 512 / THREADS;
   // dynamic shared memory for M retained columns: transform buffers, held z1,
   // two staging buffers
   static size_t smem(int M) {
@@ -611,7 +613,7 @@ struct PipeB {
 
 // pass B runs as k_passB_pipe where it applies
 template <typename T, int N>
-constexpr bool kPipeB = sizeof(T) == 4 && PassNT<T, N>::value == 2 && PipeB<N>::THREADS >= 256 &&
+constexpr bool kPipeB = sizeof(T) == 4 && PassNT<T, N>::value == 2 && PipeB<N>::THREADS >= 64 &&
                         PipeB<N>::THREADS <= 512;
 
 // Row t (0/1) of the staged pair at column kk: S holds float4 (row 0, row 1).

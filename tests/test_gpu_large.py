@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 def _case(n, seed):
     _, cp = params(n, omega=2.0, nu=1e-5, nuv=1e-5, hnu=0.1, hnuv=0.1, iflow=0)
-    g, ps, vz = random_state(n, seed, kmax_shell=100.0, slope=-3.0, amp=float(n) ** 2)
+    g, ps, vz = random_state(n, seed, kmax_shell=min(100.0, n / 3.0), slope=-3.0, amp=float(n) ** 2)
     fp, fz = random_forcing(g, seed + 1, 20.0, 22.0)
     return cp, ps, vz, fp, fz
 
@@ -30,7 +30,7 @@ def _advance(gpu, prec, cp, ps, vz, fp, fz, nsteps, mode, val):
     return a, b, t, dt
 
 
-@pytest.mark.parametrize("n", [2048, 4096])
+@pytest.mark.parametrize("n", [512, 1024, 2048, 4096])
 def test_fp32_cfl_steps_match_fp64(gpu, n):
     cp, ps, vz, fp, fz = _case(n, 7)
     a32, b32, t32, dt32 = _advance(gpu, 1, cp, ps, vz, fp, fz, 3, gpu.DT_CFL, 0.5)
@@ -84,11 +84,11 @@ def test_fp32_vs_fp64_at_8192_spectra(gpu):
     assert np.max(np.abs(ek32[live] - ek64[live]) / ek64[live]) < 1e-3
 
 
-def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch):
+@pytest.mark.parametrize("n", [512, 1024, 4096])
+def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     """The plan autotuner times the pass-B launch schedules at context
     creation; both schedules give bit-identical steps, so the choice never
     changes results."""
-    n = 4096
     cp, ps, vz, fp, fz = _case(n, 11)
     c = gpu.Context(cp, 1)
     rep = c.plan_report()
