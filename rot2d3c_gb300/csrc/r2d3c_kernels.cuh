@@ -70,12 +70,12 @@ template <typename T, int N> struct PassNT {
   static constexpr int value = (sizeof(T) == 4 && N <= 4096) ? 2 : 1;
 };
 
-// Elements per thread of pass A: radix-16 (256 threads, room for 255
-// registers, two exchanges per transform) for the FP32 4096 grid, where it
-// measured faster; the default radix elsewhere.  Pass A then needs the
-// twiddle table of its own stage schedule.
+// Elements per thread of pass A: radix-16 (up to 255 registers, fewer
+// exchanges per transform) for the FP32 grids 1024-4096, where it measured
+// faster; the default radix elsewhere.  Pass A then needs the twiddle table
+// of its own stage schedule.
 template <typename T, int N> struct PassAE {
-  static constexpr int value = (sizeof(T) == 4 && N == 4096) ? 16 : Cfg<T, N>::E;
+  static constexpr int value = (sizeof(T) == 4 && N >= 1024 && N <= 4096) ? 16 : Cfg<T, N>::E;
 };
 // (pass A keeps the two transforms' exchange buffers separate: with its 255
 // registers the interleaved float4 exchange measured slower)
