@@ -546,13 +546,15 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
 }
 
 // --------------------------------------------------------------------------
-// Pass B, FP32 pair-tiled grids with one transform group per CTA (n = 2048,
-// 4096): persistent CTAs that stage each row pair's mixed-plane inputs in
+// Pass B, FP32 pair-tiled grids (n = 512 .. 4096), one row pair per CTA at a
+// time: persistent CTAs that stage each row pair's mixed-plane inputs in
 // shared memory with asynchronous copies (cp.async, 16 bytes per thread and
 // instruction) one plane pair ahead of the transform that needs it, so that
 // the global loads of pairs 2 and 3 and of the next row pair's pair 1 overlap
-// the x-transforms instead of stalling them.  Same arithmetic, in the same
-// order, as k_passB: results are bit-identical.
+// the x-transforms instead of stalling them.  The four transforms of a row
+// pair run through one rolled copy of the transform code.  Same arithmetic,
+// in the same order, as k_passB: results are bit-identical (the launch
+// autotuner chooses between the two).
 //
 // Shared memory: the transform buffers (2 x SMEM_ELEMS), the held z1
 // (2 x N) and two staging buffers S0, S1 of one plane pair each (2 x M
