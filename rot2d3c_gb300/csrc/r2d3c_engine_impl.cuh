@@ -898,14 +898,30 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       constexpr int NT = PassNT<T, N>::value;
       using C = Cfg<T, N, NT>;
-      auto k = k_passC<T, N>;
-      const int groups = (gd_.M + NT - 1) / NT;
-      const dim3 grid((groups + C::G - 1) / C::G, nb);
-      k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ], pbase_[P_FP],
-                                           pbase_[P_FZ], c1out, c2out, gd_, d_sc_, scal_base_, o, tw_, batch(),
-                                           closure_on_ ? pbase_[P_T5] : nullptr,
-                                           closure_on_ ? pbase_[P_T6] : nullptr);
-      post("k_passC");
+      const cpx<T>* t5 = closure_on_ ? pbase_[P_T5] : nullptr;
+      const cpx<T>* t6 = closure_on_ ? pbase_[P_T6] : nullptr;
+      bool persistent = false;
+      if constexpr (kPipeC<T, N>) {
+        if (passc_mode_ == 1) {
+          // persistent: the autotuned CTA count
+          persistent = true;
+          const int pairs = (gd_.M + 1) / 2;
+          const int per_run = std::max(1, std::min(pairs, (pipec_grid_ + nb - 1) / nb));
+          k_passC_pipe<N><<<dim3(per_run, nb), PipeC<N>::THREADS, PipeC<N>::SMEM, st_>>>(
+              pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ], pbase_[P_FP], pbase_[P_FZ], c1out, c2out, gd_, d_sc_,
+              scal_base_, o, tw_, batch(), t5, t6);
+          post("k_passC_pipe");
+        }
+      }
+      if (!persistent) {  // one CTA (group) per column pair
+        auto k = k_passC<T, N>;
+        const int groups = (gd_.M + NT - 1) / NT;
+        const dim3 grid((groups + C::G - 1) / C::G, nb);
+        k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ],
+                                                           pbase_[P_FP], pbase_[P_FZ], c1out, c2out, gd_, d_sc_,
+                                                           scal_base_, o, tw_, batch(), t5, t6);
+        post("k_passC");
+      }
     });
   }
 
@@ -925,6 +941,20 @@ class EngineT final : public IEngine {
       set_smem_attr(k_passB<T, N, true>, smh);
       set_smem_attr(k_passB<T, N, false>, smh);
       set_smem_attr(k_passC<T, N>, smh);
+      if constexpr (kPipeC<T, N>) {
+        set_smem_attr(k_passC_pipe<N>, PipeC<N>::SMEM);
+        cuda_check(cudaFuncSetAttribute(k_passC_pipe<N>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                        (int)cudaSharedmemCarveoutMaxShared),
+                   "cudaFuncSetAttribute(carveout)");
+        int per_sm = 0, sms = 0, dev = 0;
+        cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_passC_pipe<N>, PipeC<N>::THREADS,
+                                                                 PipeC<N>::SMEM),
+                   "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+        if (per_sm < 1) throw Error(kEINVAL, "pass C pipeline does not fit on this device");
+        pipec_ctas_ = per_sm * sms;
+      }
       if constexpr (kPipeB<T, N>) {
         const size_t smp = PipeB<N>::smem(gd_.M);
         set_smem_attr(k_passB_pipe<N, true>, smp);
@@ -1001,6 +1031,55 @@ class EngineT final : public IEngine {
         pipeb_grid_ = pick.grid;
         launches_ = saved;
       }
+      if constexpr (kPipeC<T, N>) {
+        // pass C on the engine's scratch planes (C1, C2 in and out), zero
+        // coefficients
+        const int saved = launches_;
+        cuda_check(cudaMemsetAsync(pb_, 0, sizeof(cpx<T>) * 2 * S_ * nb_, st_), "memset");
+        cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
+        int sms = 0;
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
+        std::vector<std::pair<int, int>> cands = {{0, 0}, {1, pipec_ctas_}};
+        if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2});
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+        cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+        float best = 0.f;
+        size_t pick = 0;
+        tune_c_.clear();
+        cpx<T>* c1 = planes_[P_C1];
+        cpx<T>* c2 = planes_[P_C2];
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+          passc_mode_ = cands[ci].first;
+          pipec_grid_ = cands[ci].second;
+          for (int i = 0; i < 2; ++i) launch_passC(c1, c2, c1, c2, 4, nb_);
+          cuda_check(cudaEventRecord(e0, st_), "cudaEventRecord");
+          for (int i = 0; i < 3; ++i) launch_passC(c1, c2, c1, c2, 4, nb_);
+          cuda_check(cudaEventRecord(e1, st_), "cudaEventRecord");
+          cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+          float ms = 0.f;
+          cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+          const float us = 1e3f * ms / 3.f;
+          tune_c_.push_back({cands[ci].first, cands[ci].second, us});
+          if (ci == 0 || us < best) {
+            best = us;
+            pick = ci;
+          }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        // R2D3C_PASSC=per_column_pair|persistent overrides the measured choice
+        if (const char* force = std::getenv("R2D3C_PASSC")) {
+          if (std::strcmp(force, "per_column_pair") == 0) pick = 0;
+          else if (std::strcmp(force, "persistent") == 0) pick = 1;
+          else throw Error(kEINVAL, "R2D3C_PASSC must be per_column_pair or persistent");
+        }
+        passc_mode_ = cands[pick].first;
+        pipec_grid_ = cands[pick].second;
+        cuda_check(cudaMemsetAsync(planes_[P_C1], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
+        cuda_check(cudaMemsetAsync(planes_[P_C2], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
+        launches_ = saved;
+      }
     });
   }
 
@@ -1014,8 +1093,17 @@ class EngineT final : public IEngine {
       r += b;
     }
     char b[160];
-    snprintf(b, sizeof b, "], \"chosen\": \"%s\", \"ctas\": %d}", passb_mode_ ? "persistent" : "per_row_pair",
+    snprintf(b, sizeof b, "], \"chosen\": \"%s\", \"ctas\": %d", passb_mode_ ? "persistent" : "per_row_pair",
              passb_mode_ ? pipeb_grid_ : 0);
+    r += b;
+    r += ", \"pass_c\": [";
+    for (size_t i = 0; i < tune_c_.size(); ++i) {
+      snprintf(b, sizeof b, "%s{\"variant\": \"%s\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
+               tune_c_[i].mode ? "persistent" : "per_column_pair", tune_c_[i].grid, (double)tune_c_[i].us);
+      r += b;
+    }
+    snprintf(b, sizeof b, "], \"chosen_c\": \"%s\", \"ctas_c\": %d}",
+             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0);
     return r + b;
   }
 
@@ -1047,11 +1135,14 @@ class EngineT final : public IEngine {
   int pipeb_ctas_ = 0;  // resident CTAs of the pipelined pass B (whole device)
   int passb_mode_ = 0;  // 0: one CTA per row pair, 1: persistent (autotuned)
   int pipeb_grid_ = 0;  // CTAs of the persistent pass B (autotuned)
+  int pipec_ctas_ = 0;  // resident CTAs of the persistent pass C (whole device)
+  int passc_mode_ = 0;  // 0: one CTA per column pair, 1: persistent (autotuned)
+  int pipec_grid_ = 0;  // CTAs of the persistent pass C (autotuned)
   struct TuneRec {
     int mode, grid;
     float us;
   };
-  std::vector<TuneRec> tune_;
+  std::vector<TuneRec> tune_, tune_c_;
   cpx<T>* pbase_[P_COUNT] = {};
   double* scal_base_ = nullptr;
   unsigned long long* enc_base_ = nullptr;

@@ -830,6 +830,108 @@ __device__ __forceinline__ void prefetch_columns_l2(const cpx<T>* p, int ncol, i
   prefetch_l2(p + (size_t)ncol * N - L, (size_t)L);
 }
 
+// The RK update of pass C for FP32 with the held c5 (FP32 grids up to 4096):
+// c6 (this thread's transform output v) joins c5 in shared memory (the
+// transform buffer sm is free after the last transform), then the threads
+// update the retained rows two at a time (rows 2p, 2p+1 of one column:
+// 16-byte loads and stores), two row pairs per iteration with all loads of
+// an iteration issued before its stores.  Each element is loaded and stored
+// by one thread.  Every thread of the CTA calls it (one barrier inside).
+template <typename T, int N, int NT, int E, int TPF>
+__device__ __forceinline__ void passC_update_pairs(cpx<T>* sm, const cpx<T>* hold, const cpx<T> (&v)[NT][E],
+                                                   int lane, int kx0, const cpx<T>* c1in, const cpx<T>* c2in,
+                                                   const cpx<T>* ps, const cpx<T>* vz, const cpx<T>* __restrict__ fp,
+                                                   const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out,
+                                                   const DevGrid& gd, const StepCoef& sc, T tmp1,
+                                                   const cpx<T>* __restrict__ tau5,
+                                                   const cpx<T>* __restrict__ tau6) {
+  cpx<T>* c6s = sm;
+#pragma unroll
+  for (int t = 0; t < NT; ++t)
+#pragma unroll
+    for (int q = 0; q < E; ++q) c6s[t * N + lane + q * TPF] = v[t][q];
+  __syncthreads();
+  const int L = gd.L;
+  const int lo_pairs = L / 2 + 1;       // pairs p = 0 .. L/2 hold rows 0 .. L
+  const int hi_first = (N - L) / 2;     // pairs hi_first .. N/2-1 hold rows N-L .. N-1
+  const int npc = lo_pairs + (N / 2 - hi_first);
+  const int total = NT * npc;
+  using F4 = float4;
+  constexpr int RB = 2;
+  auto ld4 = [](const cpx<T>* base, size_t idx) { return *reinterpret_cast<const F4*>(base + idx); };
+#pragma unroll 1
+  for (int e0 = lane; e0 < total; e0 += RB * TPF) {
+    F4 a1[RB], a2[RB], p0[RB], f0[RB], v0[RB], g0[RB];
+    int col[RB], j0[RB];
+    bool keep[RB][2], in[RB][2];
+#pragma unroll
+    for (int b = 0; b < RB; ++b) {
+      const int e = e0 + b * TPF;
+      const int t = e / npc, pi = e % npc;
+      const int pr = pi < lo_pairs ? pi : hi_first + (pi - lo_pairs);
+      col[b] = kx0 + t;
+      j0[b] = 2 * pr;
+      bool any = false;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int ky = ky_of(j0[b] + h, N), k2 = col[b] * col[b] + ky * ky;
+        keep[b][h] = e < total && col[b] < gd.M && ky <= L && -ky <= L;
+        in[b][h] = keep[b][h] && k2 <= gd.kmaxi && k2 >= 1;
+        any |= in[b][h];
+      }
+      if (any) {
+        const size_t idx = (size_t)col[b] * N + j0[b];
+        a1[b] = ld4(c1in, idx);
+        a2[b] = ld4(c2in, idx);
+        p0[b] = ld4(ps, idx);
+        f0[b] = ld4(fp, idx);
+        v0[b] = ld4(vz, idx);
+        g0[b] = ld4(fz, idx);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < RB; ++b) {
+      if (!keep[b][0] && !keep[b][1]) continue;
+      const int t = col[b] - kx0;
+      const size_t idx = (size_t)col[b] * N + j0[b];
+      // the two rows of the pair: h = 0 (x, y halves of the float4s), h = 1 (z, w)
+      auto row = [&](int h, cpx<T>& n1, cpx<T>& n2) {
+        n1 = czero<T>();
+        n2 = czero<T>();
+        if (!in[b][h]) return;
+        const int ky = ky_of(j0[b] + h, N), k2 = col[b] * col[b] + ky * ky;
+        RkIn<T> r;
+        r.a1 = h ? mkc<T>(a1[b].z, a1[b].w) : mkc<T>(a1[b].x, a1[b].y);
+        r.a2 = h ? mkc<T>(a2[b].z, a2[b].w) : mkc<T>(a2[b].x, a2[b].y);
+        r.p0 = h ? mkc<T>(p0[b].z, p0[b].w) : mkc<T>(p0[b].x, p0[b].y);
+        r.f0 = h ? mkc<T>(f0[b].z, f0[b].w) : mkc<T>(f0[b].x, f0[b].y);
+        r.v0 = h ? mkc<T>(v0[b].z, v0[b].w) : mkc<T>(v0[b].x, v0[b].y);
+        r.g0 = h ? mkc<T>(g0[b].z, g0[b].w) : mkc<T>(g0[b].x, g0[b].y);
+        cpx<T> c5 = hold[t * N + j0[b] + h], c6 = c6s[t * N + j0[b] + h];
+        if (tau5) {  // learned subgrid tendencies of the two brackets
+          const cpx<T> u = tau5[idx + h], w = tau6[idx + h];
+          c5 = mkc<T>(c5.x + u.x, c5.y + u.y);
+          c6 = mkc<T>(c6.x + w.x, c6.y + w.y);
+        }
+        rk_apply<T>(r, c5, c6, ky, k2, sc, tmp1, n1, n2);
+      };
+      cpx<T> n10, n20, n11, n21;
+      row(0, n10, n20);
+      row(1, n11, n21);
+      if (keep[b][0] && keep[b][1]) {
+        *reinterpret_cast<F4*>(c1out + idx) = make_float4(n10.x, n10.y, n11.x, n11.y);
+        *reinterpret_cast<F4*>(c2out + idx) = make_float4(n20.x, n20.y, n21.x, n21.y);
+      } else if (keep[b][0]) {
+        c1out[idx] = n10;
+        c2out[idx] = n20;
+      } else {
+        c1out[idx + 1] = n11;
+        c2out[idx + 1] = n21;
+      }
+    }
+  }
+}
+
 template <typename T, int N>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
@@ -921,96 +1023,8 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   const StepCoef sc = scs[blockIdx.y];
   const T tmp1 = (T)(scal[blockIdx.y * kScalStride] / (double)o);  // :581
   if constexpr (HOLD && sizeof(T) == 4) {
-    // FP32: c6 joins c5 in shared memory (the transform buffer is free after
-    // the last transform), then the threads update the retained rows two at a
-    // time (rows 2p, 2p+1 of one column: 16-byte loads and stores), two row
-    // pairs per iteration with all loads of an iteration issued before its
-    // stores.  Each element is still loaded and stored by one thread.
-    cpx<T>* c6s = sm;
-#pragma unroll
-    for (int t = 0; t < NT; ++t)
-#pragma unroll
-      for (int q = 0; q < C::E; ++q) c6s[t * N + lane + q * C::TPF] = v[t][q];
-    __syncthreads();
-    const int L = gd.L;
-    const int lo_pairs = L / 2 + 1;       // pairs p = 0 .. L/2 hold rows 0 .. L
-    const int hi_first = (N - L) / 2;     // pairs hi_first .. N/2-1 hold rows N-L .. N-1
-    const int npc = lo_pairs + (N / 2 - hi_first);
-    const int total = NT * npc;
-    using F4 = float4;
-    constexpr int RB = 2;
-    auto ld4 = [](const cpx<T>* base, size_t idx) { return *reinterpret_cast<const F4*>(base + idx); };
-#pragma unroll 1
-    for (int e0 = lane; e0 < total; e0 += RB * C::TPF) {
-      F4 a1[RB], a2[RB], p0[RB], f0[RB], v0[RB], g0[RB];
-      int col[RB], j0[RB];
-      bool keep[RB][2], in[RB][2];
-#pragma unroll
-      for (int b = 0; b < RB; ++b) {
-        const int e = e0 + b * C::TPF;
-        const int t = e / npc, pi = e % npc;
-        const int pr = pi < lo_pairs ? pi : hi_first + (pi - lo_pairs);
-        col[b] = kx0 + t;
-        j0[b] = 2 * pr;
-        bool any = false;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int ky = ky_of(j0[b] + h, N), k2 = col[b] * col[b] + ky * ky;
-          keep[b][h] = e < total && col[b] < gd.M && ky <= L && -ky <= L;
-          in[b][h] = keep[b][h] && k2 <= gd.kmaxi && k2 >= 1;
-          any |= in[b][h];
-        }
-        if (any) {
-          const size_t idx = (size_t)col[b] * N + j0[b];
-          a1[b] = ld4(c1in, idx);
-          a2[b] = ld4(c2in, idx);
-          p0[b] = ld4(ps, idx);
-          f0[b] = ld4(fp, idx);
-          v0[b] = ld4(vz, idx);
-          g0[b] = ld4(fz, idx);
-        }
-      }
-#pragma unroll
-      for (int b = 0; b < RB; ++b) {
-        if (!keep[b][0] && !keep[b][1]) continue;
-        const int t = col[b] - kx0;
-        const size_t idx = (size_t)col[b] * N + j0[b];
-        // the two rows of the pair: h = 0 (x, y halves of the float4s), h = 1 (z, w)
-        auto row = [&](int h, cpx<T>& n1, cpx<T>& n2) {
-          n1 = czero<T>();
-          n2 = czero<T>();
-          if (!in[b][h]) return;
-          const int ky = ky_of(j0[b] + h, N), k2 = col[b] * col[b] + ky * ky;
-          RkIn<T> r;
-          r.a1 = h ? mkc<T>(a1[b].z, a1[b].w) : mkc<T>(a1[b].x, a1[b].y);
-          r.a2 = h ? mkc<T>(a2[b].z, a2[b].w) : mkc<T>(a2[b].x, a2[b].y);
-          r.p0 = h ? mkc<T>(p0[b].z, p0[b].w) : mkc<T>(p0[b].x, p0[b].y);
-          r.f0 = h ? mkc<T>(f0[b].z, f0[b].w) : mkc<T>(f0[b].x, f0[b].y);
-          r.v0 = h ? mkc<T>(v0[b].z, v0[b].w) : mkc<T>(v0[b].x, v0[b].y);
-          r.g0 = h ? mkc<T>(g0[b].z, g0[b].w) : mkc<T>(g0[b].x, g0[b].y);
-          cpx<T> c5 = hold[t * N + j0[b] + h], c6 = c6s[t * N + j0[b] + h];
-          if (tau5) {  // learned subgrid tendencies of the two brackets
-            const cpx<T> u = tau5[idx + h], w = tau6[idx + h];
-            c5 = mkc<T>(c5.x + u.x, c5.y + u.y);
-            c6 = mkc<T>(c6.x + w.x, c6.y + w.y);
-          }
-          rk_apply<T>(r, c5, c6, ky, k2, sc, tmp1, n1, n2);
-        };
-        cpx<T> n10, n20, n11, n21;
-        row(0, n10, n20);
-        row(1, n11, n21);
-        if (keep[b][0] && keep[b][1]) {
-          *reinterpret_cast<F4*>(c1out + idx) = make_float4(n10.x, n10.y, n11.x, n11.y);
-          *reinterpret_cast<F4*>(c2out + idx) = make_float4(n20.x, n20.y, n21.x, n21.y);
-        } else if (keep[b][0]) {
-          c1out[idx] = n10;
-          c2out[idx] = n20;
-        } else {
-          c1out[idx + 1] = n11;
-          c2out[idx + 1] = n21;
-        }
-      }
-    }
+    passC_update_pairs<T, N, NT, C::E, C::TPF>(sm, hold, v, lane, kx0, c1in, c2in, ps, vz, fp, fz, c1out, c2out, gd,
+                                                sc, tmp1, tau5, tau6);
   } else if constexpr (HOLD) {
     // c6 joins c5 in shared memory (the transform buffer is free after the
     // last transform; each thread reads back only what it wrote), and the
@@ -1088,6 +1102,118 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
       }
     }
   }
+}
+
+// --------------------------------------------------------------------------
+// Pass C, FP32 pair-tiled grids (n = 512 .. 4096): persistent CTAs, one
+// column pair at a time.  Each bracket plane's two columns are staged in
+// shared memory by cp.async (32 contiguous bytes per row pair: rows 2p, 2p+1
+// of both columns) while the previous transform runs: plane 1 during plane
+// 0's transform, the next column pair's plane 0 during plane 1's transform
+// and the RK update.  The RK inputs of the column pair are prefetched into
+// L2 when its turn starts.  Same arithmetic as k_passC (bit-identical; the
+// launch autotuner chooses between the two).
+// --------------------------------------------------------------------------
+template <int N>
+struct PipeC {
+  using C = Cfg<float, N, 2>;
+  using F = typename C::FFT;
+  static constexpr int TPF = C::TPF, THREADS = TPF;
+  static constexpr int MINB = 512 / THREADS;  // 16 warps per SM at 128 registers
+  // transform buffers, held c5 (2 columns), one staged plane (2 columns)
+  static constexpr size_t SMEM = (size_t)2 * F::SMEM_ELEMS * sizeof(float2) + (size_t)4 * N * sizeof(float2);
+};
+template <typename T, int N>
+constexpr bool kPipeC = sizeof(T) == 4 && PassNT<T, N>::value == 2 && PassSmem<T, N>::HOLD &&
+                        PipeC<N>::THREADS >= 64 && PipeC<N>::THREADS <= 512;
+
+template <int N>
+__global__ void __launch_bounds__(PipeC<N>::THREADS, PipeC<N>::MINB)
+k_passC_pipe(const float2* __restrict__ pb, const float2* c1in, const float2* c2in, const float2* ps,
+             const float2* vz, const float2* __restrict__ fp, const float2* __restrict__ fz, float2* c1out,
+             float2* c2out, DevGrid gd, const StepCoef* __restrict__ scs, const double* __restrict__ scal, int o,
+             const float4* __restrict__ tw, Batch bs, const float2* __restrict__ tau5,
+             const float2* __restrict__ tau6) {
+  using T = float;
+  constexpr int NT = 2;
+  using PC = PipeC<N>;
+  using F = typename PC::F;
+  constexpr int TPF = PC::TPF, E = PC::C::E;
+  const size_t rs = blockIdx.y * bs.spec;
+  pb += blockIdx.y * bs.pb;
+  c1in += rs;
+  c2in += rs;
+  ps += rs;
+  vz += rs;
+  fp += rs;
+  fz += rs;
+  c1out += rs;
+  c2out += rs;
+  R2D3C_SMEM_DECL
+  const int lane0 = threadIdx.x;
+  cpx<T>* sm = smbase_;
+  cpx<T>* hold = sm + NT * F::SMEM_ELEMS;
+  float4* S4 = reinterpret_cast<float4*>(hold + NT * N);  // [row pair][column] = rows 2p, 2p+1
+  const size_t oplane = (size_t)gd.nh * N;
+  const int npairs = (gd.M + 1) / 2;
+  // plane pl of column pair cp into S4 (one commit group; empty when !on)
+  auto stage = [&](int pl, int cp, bool on) {
+    if (on) {
+      const float4* src = reinterpret_cast<const float4*>(pb + pl * oplane) + 2 * cp;  // ((p*nh + kx0)*2) / 2
+      for (int i = threadIdx.x; i < N; i += TPF) {
+        const int p = i >> 1, h = i & 1;
+        cp_async16(S4 + i, src + (size_t)p * gd.nh + h);
+      }
+    }
+    cp_async_commit();
+  };
+  int cp = blockIdx.x;
+  if (cp >= npairs) return;  // uniform for the whole CTA
+  stage(0, cp, true);
+  for (; cp < npairs; cp += gridDim.x) {
+    const int kx0 = 2 * cp;
+    const int nx = cp + gridDim.x;
+    if (lane0 < 8) {  // the RK update's inputs into L2 while the transforms run
+      const int lane = lane0;
+      const cpx<T>* src = lane == 0 ? c1in : lane == 1 ? c2in : lane == 2 ? ps : lane == 3 ? vz
+                        : lane == 4 ? fp : lane == 5 ? fz : lane == 6 ? tau5 : tau6;
+      const int ncol = min(NT, gd.M - kx0);
+      if (src && ncol > 0) prefetch_columns_l2<T>(src + (size_t)kx0 * N, ncol, N, gd.L);
+    }
+    cpx<T> v[NT][E];
+#pragma unroll 1
+    for (int pl = 0; pl < 2; ++pl) {
+      // addresses derived from an opaque lane index: not hoisted out of the
+      // loop into registers held across it
+      const int lane = opaque(lane0);
+      cp_async_wait<0>();
+      __syncthreads();  // plane pl staged; previous users of sm and hold done
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int y = lane + q * TPF;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+          const float4 w = S4[(y >> 1) * 2 + t];
+          v[t][q] = (y & 1) ? mkc<T>(w.z, w.w) : mkc<T>(w.x, w.y);
+        }
+      }
+      __syncthreads();  // every read of S4 done
+      if (pl == 0) stage(1, cp, true);
+      else stage(0, nx, nx < npairs);
+      F::template run<-1>(v, lane, sm, tw);
+      if (pl == 0) {
+#pragma unroll
+        for (int t = 0; t < NT; ++t)
+#pragma unroll
+          for (int q = 0; q < E; ++q) hold[t * N + lane + q * TPF] = v[t][q];
+      }
+    }
+    const StepCoef sc = scs[blockIdx.y];
+    const T tmp1 = (T)(scal[blockIdx.y * kScalStride] / (double)o);  // :581
+    passC_update_pairs<T, N, NT, E, TPF>(sm, hold, v, lane0, kx0, c1in, c2in, ps, vz, fp, fz, c1out, c2out, gd,
+                                         sc, tmp1, tau5, tau6);
+  }
+  cp_async_wait<0>();  // no copy outlives the CTA
 }
 
 }  // namespace r2d3c

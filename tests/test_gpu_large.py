@@ -94,12 +94,15 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     rep = c.plan_report()
     assert {r["variant"] for r in rep["pass_b"]} == {"per_row_pair", "persistent"}
     assert all(r["us"] > 0 for r in rep["pass_b"]) and rep["chosen"] in ("per_row_pair", "persistent")
+    assert {r["variant"] for r in rep["pass_c"]} == {"per_column_pair", "persistent"}
+    assert all(r["us"] > 0 for r in rep["pass_c"]) and rep["chosen_c"] in ("per_column_pair", "persistent")
     c.destroy()
     out = []
-    for mode in ("per_row_pair", "persistent"):
-        monkeypatch.setenv("R2D3C_PASSB", mode)
+    for mb, mc in (("per_row_pair", "per_column_pair"), ("persistent", "persistent")):
+        monkeypatch.setenv("R2D3C_PASSB", mb)
+        monkeypatch.setenv("R2D3C_PASSC", mc)
         c = gpu.Context(cp, 1)
-        assert c.plan_report()["chosen"] == mode
+        assert c.plan_report()["chosen"] == mb and c.plan_report()["chosen_c"] == mc
         c.set_state(ps, vz)
         c.set_forcing(fp, fz)
         c.set_time(0.0)
@@ -108,5 +111,6 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
         c.destroy()
     for u, v in zip(out[0], out[1]):
         np.testing.assert_array_equal(u, v)
-    small = gpu.Context(params(64, iflow=0)[1], 1)
-    assert small.plan_report() == {"pass_b": [], "chosen": "per_row_pair", "ctas": 0}
+    small = gpu.Context(params(64, iflow=0)[1], 1).plan_report()
+    assert small["pass_b"] == [] and small["chosen"] == "per_row_pair"
+    assert small["pass_c"] == [] and small["chosen_c"] == "per_column_pair"
