@@ -23,6 +23,10 @@ enum SpecOp : int {
 // kx value of spectral column i (ka(i), Rot2D3C.para.f90:220-223)
 __device__ __forceinline__ int kx_of(int i, int n) { return i < (n >> 1) ? i : i - n; }
 
+struct Scale8 {
+  double v[8];
+};
+
 template <typename T>
 __global__ void k_specop(const cpx<T>* __restrict__ a, cpx<T>* __restrict__ b, DevGrid gd, int op,
                          double s) {
@@ -518,6 +522,59 @@ __global__ void k_to_channel(const T* __restrict__ r, size_t count, double s, fl
                              int ch) {
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < count; p += (size_t)gridDim.x * blockDim.x)
     out[p * nch + ch] = (float)((double)r[p] * s);
+}
+
+// The 8 spectral fields of the closure's inputs from psi and vz in one pass
+// (the specop chain of closure_inputs, same arithmetic): planes c = 0..7 of
+// w8 (S elements each) = -k^2 psi, vz, d_x psi, d_y psi, d_x(-k^2 psi),
+// d_y(-k^2 psi), d_x vz, d_y vz; every field but the first masked to
+// k^2 <= kmax (the first is psi's own truncation).
+template <typename T>
+__global__ void k_closure_specs(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, DevGrid gd,
+                                cpx<T>* __restrict__ w8) {
+  const size_t total = (size_t)gd.nh * gd.n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
+    const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
+    const int k2 = kx * kx + ky * ky;
+    const bool in = k2 <= gd.kmaxi;
+    const cpx<T> x = ps[idx], z = vz[idx];
+    const T m = -(T)k2;
+    const cpx<T> L = mkc<T>(m * x.x, m * x.y);
+    const T fx = (T)kx, fy = (T)ky;
+    const cpx<T> zero = czero<T>();
+    w8[idx] = L;
+    w8[total + idx] = in ? z : zero;
+    w8[2 * total + idx] = in ? mkc<T>(-fx * x.y, fx * x.x) : zero;
+    w8[3 * total + idx] = in ? mkc<T>(-fy * x.y, fy * x.x) : zero;
+    w8[4 * total + idx] = in ? mkc<T>(-fx * L.y, fx * L.x) : zero;
+    w8[5 * total + idx] = in ? mkc<T>(-fy * L.y, fy * L.x) : zero;
+    w8[6 * total + idx] = in ? mkc<T>(-fx * z.y, fx * z.x) : zero;
+    w8[7 * total + idx] = in ? mkc<T>(-fy * z.y, fy * z.x) : zero;
+  }
+}
+
+// out[p*8 + c] = r8[c*count + p] * s[c]  (8 real planes -> FP32 NHWC)
+template <typename T>
+__global__ void k_to_channels8(const T* __restrict__ r8, size_t count, Scale8 s, float* __restrict__ out) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < count; p += (size_t)gridDim.x * blockDim.x) {
+    float o[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) o[c] = (float)((double)r8[c * count + p] * s.v[c]);
+    reinterpret_cast<float4*>(out + p * 8)[0] = make_float4(o[0], o[1], o[2], o[3]);
+    reinterpret_cast<float4*>(out + p * 8)[1] = make_float4(o[4], o[5], o[6], o[7]);
+  }
+}
+
+// r2[c*count + p] = in[p*2 + c], c = 0, 1  (FP32 NHWC, 2 channels -> 2 real planes)
+template <typename T>
+__global__ void k_from_channels2(const float* __restrict__ in, size_t count, T* __restrict__ r2) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < count; p += (size_t)gridDim.x * blockDim.x) {
+    const float2 v = reinterpret_cast<const float2*>(in)[p];
+    r2[p] = (T)v.x;
+    r2[count + p] = (T)v.y;
+  }
 }
 
 // r[p] = in[p*nch + ch]

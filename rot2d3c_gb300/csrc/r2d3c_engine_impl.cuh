@@ -551,22 +551,29 @@ class EngineT final : public IEngine {
     hook_ = id ? std::move(hook) : nullptr;
     hook_id_ = id;
   }
+  // scratch of the closure's batched transforms: 8 spectral planes, 8 mixed
+  // planes, 8 real planes (allocated once, outside any stream capture)
+  void closure_scratch() {
+    if (cl_w8_) return;
+    cl_w8_ = alloc<cpx<T>>(8 * S_);
+    cl_t8_ = alloc<cpx<T>>(8 * S_);
+    cl_r8_ = alloc<T>((size_t)8 * n_ * n_);
+  }
   void closure_inputs(float* d_x, bool wait) override {
+    // omega = -lap psi = k^2 psi, vz, d/dx and d/dy of psi, omega, vz: the 8
+    // spectral fields in one pass, one batched C2R (columns, then rows), one
+    // interleave into the FP32 NHWC tensor scaled by 1/n^2
+    if (wait) closure_scratch();
+    if (!cl_w8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
     const size_t cnt = (size_t)n_ * n_;
     const double s = 1.0 / ((double)n_ * n_);
-    // omega = -lap psi = k^2 psi: -(laplak2 psi); vz; d/dx, d/dy of psi, omega, vz
-    struct Ch { int src, op1, op2; double sign; };
-    const Ch ch[8] = {{P_PS, OP_LAPLA, -1, -1.0}, {P_VZ, OP_COPY_MASK, -1, 1.0},
-                      {P_PS, OP_DERIV_X, -1, 1.0}, {P_PS, OP_DERIV_Y, -1, 1.0},
-                      {P_PS, OP_LAPLA, OP_DERIV_X, -1.0}, {P_PS, OP_LAPLA, OP_DERIV_Y, -1.0},
-                      {P_VZ, OP_DERIV_X, -1, 1.0}, {P_VZ, OP_DERIV_Y, -1, 1.0}};
-    for (int c = 0; c < 8; ++c) {
-      specop(ch[c].src, P_W2, ch[c].op1, 0.0);
-      if (ch[c].op2 >= 0) specop(P_W2, P_W1, ch[c].op2, 0.0);
-      c2r(ch[c].op2 >= 0 ? P_W1 : P_W2, R_1, nullptr, nullptr);
-      k_to_channel<T><<<elem_blocks(cnt), 256, 0, st_>>>(rplanes_[R_1], cnt, ch[c].sign * s, d_x, 8, c);
-      post("k_to_channel");
-    }
+    k_closure_specs<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[P_PS], planes_[P_VZ], gd_, cl_w8_);
+    post("k_closure_specs");
+    launch_colfft<+1>(cl_w8_, cl_t8_, 8 * gd_.nh);
+    launch_rowc2r(cl_t8_, cl_r8_, nullptr, 8);
+    const Scale8 sc{{-s, s, s, s, -s, -s, s, s}};
+    k_to_channels8<T><<<elem_blocks(cnt), 256, 0, st_>>>(cl_r8_, cnt, sc, d_x);
+    post("k_to_channels8");
     if (wait) sync();
   }
   void brackets() override { brackets_full(); }
@@ -608,12 +615,16 @@ class EngineT final : public IEngine {
       return;
     }
     if (nb_ != 1) throw Error(kEINVAL, "the closure is a single-run feature");
+    if (wait) closure_scratch();
+    if (!cl_w8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
+    // the two channels as two real planes, one batched row R2C, the column
+    // transforms into the tendency planes
     const size_t cnt = (size_t)n_ * n_;
-    for (int c = 0; c < 2; ++c) {
-      k_from_channel<T><<<elem_blocks(cnt), 256, 0, st_>>>(d_t, 2, c, cnt, rplanes_[R_1]);
-      post("k_from_channel");
-      r2c(R_1, c == 0 ? P_T5 : P_T6);
-    }
+    k_from_channels2<T><<<elem_blocks(cnt), 256, 0, st_>>>(d_t, cnt, cl_r8_);
+    post("k_from_channels2");
+    launch_rowr2c(cl_r8_, cl_t8_, 2);
+    launch_colfft<-1>(cl_t8_, planes_[P_T5], gd_.nh);
+    launch_colfft<-1>(cl_t8_ + S_, planes_[P_T6], gd_.nh);
     // the tendency planes are fixed buffers: a captured step keyed on
     // closure_on_ stays valid across calls
     closure_on_ = true;
@@ -832,21 +843,22 @@ class EngineT final : public IEngine {
       post("k_colfft");
     });
   }
-  void launch_rowc2r(const cpx<T>* tin, T* rout, unsigned long long* mm) {
+  // nplanes consecutive planes at once (blockIdx.y = plane)
+  void launch_rowc2r(const cpx<T>* tin, T* rout, unsigned long long* mm, int nplanes = 1) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       using C = Cfg<T, N>;
       auto k = k_rowc2r<T, N>;
-      k<<<(N / 2 + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(tin, rout, mm, tw_);
+      k<<<dim3((N / 2 + C::G - 1) / C::G, nplanes), C::THREADS, C::SMEM, st_>>>(tin, rout, mm, tw_);
       post("k_rowc2r");
     });
   }
-  void launch_rowr2c(const T* rin, cpx<T>* tout) {
+  void launch_rowr2c(const T* rin, cpx<T>* tout, int nplanes = 1) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       using C = Cfg<T, N>;
       auto k = k_rowr2c<T, N>;
-      k<<<(N / 2 + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(rin, tout, tw_);
+      k<<<dim3((N / 2 + C::G - 1) / C::G, nplanes), C::THREADS, C::SMEM, st_>>>(rin, tout, tw_);
       post("k_rowr2c");
     });
   }
@@ -1130,6 +1142,9 @@ class EngineT final : public IEngine {
   bool full_;
   int nb_ = 1, run_ = 0;
   bool closure_on_ = false;
+  cpx<T>* cl_w8_ = nullptr;  // closure scratch (closure_scratch)
+  cpx<T>* cl_t8_ = nullptr;
+  T* cl_r8_ = nullptr;
   std::function<void(cudaStream_t)> hook_;
   unsigned long long hook_id_ = 0;
   int pipeb_ctas_ = 0;  // resident CTAs of the pipelined pass B (whole device)

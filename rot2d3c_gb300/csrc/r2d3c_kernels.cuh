@@ -191,6 +191,9 @@ k_rowc2r(const cpx<T>* __restrict__ tin, T* __restrict__ rout,
   using C = Cfg<T, N>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
+  // blockIdx.y: plane of a batch of consecutive mixed / real planes
+  tin += blockIdx.y * (size_t)(N / 2 + 1) * N;
+  if (rout) rout += blockIdx.y * (size_t)N * N;
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
   int pair = blockIdx.x * C::G + g;
@@ -251,6 +254,9 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
   using C = Cfg<T, N>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
+  // blockIdx.y: plane of a batch of consecutive real / mixed planes
+  rin += blockIdx.y * (size_t)N * N;
+  tout += blockIdx.y * (size_t)(N / 2 + 1) * N;
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
   int pair = blockIdx.x * C::G + g;
