@@ -290,11 +290,15 @@ struct TcConv {
   static constexpr int HALO_UNITS = 3 * NCH * (kTcPix + 2);
   static constexpr int W_UNITS = 9 * CIN * COUT / 8;
   // output staging of one tile: y [128][COUT] f32 and a [128][COUT] bf16,
-  // 16-byte chunks XOR-swizzled within each pixel row
+  // 16-byte chunks XOR-swizzled within each pixel row.  It reuses the tile's
+  // own halo buffer (free once the MMAs have completed) when it fits, else
+  // it has its own region.
   static constexpr int Y_UNITS = kTcPix * COUT / 4, A_UNITS = kTcPix * COUT / 8;
+  static constexpr bool STAGE_IN_HALO = Y_UNITS + A_UNITS <= HALO_UNITS;
+  static constexpr int STAGE_UNITS = STAGE_IN_HALO ? 0 : Y_UNITS + A_UNITS;
   // two halo buffers (the next tile's is copied while this one's runs), the
   // weights, the output staging, the mbarrier and the TMEM address
-  static constexpr size_t SMEM = (size_t)(2 * HALO_UNITS + W_UNITS + Y_UNITS + A_UNITS) * 16 + 64;
+  static constexpr size_t SMEM = (size_t)(2 * HALO_UNITS + W_UNITS + STAGE_UNITS) * 16 + 64;
 };
 
 // halo of tile t into buffer dst (one cp.async commit group; empty when
@@ -327,9 +331,8 @@ k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float*
   extern __shared__ __align__(128) unsigned char tc_smem[];
   uint4* s_halo = reinterpret_cast<uint4*>(tc_smem);  // two buffers
   uint4* s_w = s_halo + 2 * TC::HALO_UNITS;
-  uint4* s_y = s_w + TC::W_UNITS;
-  uint4* s_a = s_y + TC::Y_UNITS;
-  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_a + TC::A_UNITS);
+  uint4* s_stage = s_w + TC::W_UNITS;  // own staging region (STAGE_UNITS)
+  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_stage + TC::STAGE_UNITS);
   unsigned* s_tmem = reinterpret_cast<unsigned*>(s_bar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // weights, already in the K-major UMMA layout: unit (kc, n) = k 8kc..8kc+7 of column n
@@ -396,6 +399,8 @@ k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float*
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     // epilogue: pixel m = 32*warp + lane of the tile, COUT accumulators
+    uint4* s_y = TC::STAGE_IN_HALO ? cur : s_stage;
+    uint4* s_a = s_y + TC::Y_UNITS;
     const int b = t / (tiles_x * H), gy = (t / tiles_x) % H, x0 = (t % tiles_x) * kTcPix;
     const size_t pix0 = ((size_t)b * H + gy) * W + x0;  // the tile's pixels are contiguous
     const int m = warp * 32 + lane;
@@ -444,7 +449,10 @@ k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float*
         ga4[q] = s_a[mm * AC + (c ^ ((mm / (8 / AC)) % AC))];
       }
     }
-    // the staging is rewritten only after the next tile's barriers
+    // the staging (possibly this tile's halo buffer, which the copy issued
+    // at the top of the next-but-one iteration refills) is free only after
+    // every thread's copy-out
+    if constexpr (TC::STAGE_IN_HALO) __syncthreads();
   }
   tc_wait<0>();  // no copy outlives the CTA
   __syncthreads();
