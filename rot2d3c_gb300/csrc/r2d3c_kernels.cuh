@@ -291,7 +291,7 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
 // both as 16-byte column pairs of the pair-tiled plane.
 // --------------------------------------------------------------------------
 template <typename T, int N>
-__global__ void __launch_bounds__(CfgA<T, N>::THREADS, 1)
+__global__ void __launch_bounds__(CfgA<T, N>::THREADS, (sizeof(T) == 4 && CfgA<T, N>::THREADS == 256) ? 2 : 1)
 k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __restrict__ tf,
         DevGrid gd, const tw_t<T>* __restrict__ tw, Batch bs) {
   constexpr int NT = PassNT<T, N>::value;
@@ -308,9 +308,10 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
   int kyi[C::E];
 #pragma unroll
   for (int q = 0; q < C::E; ++q) kyi[q] = ky_of(lane + q * C::TPF, N);
-  // FP32 keeps the source column pair in registers across its fields; FP64
-  // (registers full) re-reads it for every field, from L2
-  constexpr bool KEEP = sizeof(T) == 4;
+  // The source column (pair) is re-read for every field, from L2, rather
+  // than held in registers across the fields: the registers freed let FP32
+  // run two 256-thread CTAs per SM (and keep FP64 from spilling)
+  constexpr bool KEEP = false;
   cpx<T> s[KEEP ? NT : 1][KEEP ? C::E : 1], v[NT][C::E];
   auto src_at = [&](const cpx<T>* sp, int t, int q) -> cpx<T> {
     const int col = kx0 + t, ky = kyi[q];
