@@ -311,8 +311,7 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
   // The source column (pair) is re-read for every field, from L2, rather
   // than held in registers across the fields: the registers freed let FP32
   // run two 256-thread CTAs per SM (and keep FP64 from spilling)
-  constexpr bool KEEP = false;
-  cpx<T> s[KEEP ? NT : 1][KEEP ? C::E : 1], v[NT][C::E];
+  cpx<T> v[NT][C::E];
   auto src_at = [&](const cpx<T>* sp, int t, int q) -> cpx<T> {
     const int col = kx0 + t, ky = kyi[q];
     const bool in = col < gd.M && (ky <= gd.L && -ky <= gd.L) && col * col + ky * ky <= gd.kmaxi;
@@ -321,12 +320,6 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
 #pragma unroll 1
   for (int src = 0; src < 2; ++src) {  // psi for fields 0-3, vz for fields 4-5
     const cpx<T>* sp = src == 0 ? ps : vz;
-    if constexpr (KEEP) {
-#pragma unroll
-      for (int t = 0; t < NT; ++t)
-#pragma unroll
-        for (int q = 0; q < C::E; ++q) s[t][q] = src_at(sp, t, q);
-    }
 #pragma unroll 1
     for (int f = src * 4; f < (src == 0 ? 4 : 6); ++f) {
 #pragma unroll
@@ -336,9 +329,7 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
         for (int q = 0; q < C::E; ++q) {
           // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
           const T k = (f & 1) ? (T)kyi[q] : (T)col;
-          cpx<T> x;
-          if constexpr (KEEP) x = s[t][q];
-          else x = src_at(sp, t, q);
+          cpx<T> x = src_at(sp, t, q);
           if (f == 2 || f == 3) {
             const T m = -(T)(col * col + kyi[q] * kyi[q]);  // laplak2: -ka2*a
             x = mkc<T>(m * x.x, m * x.y);
