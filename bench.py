@@ -388,10 +388,14 @@ def cpu_baseline(n, ps, vz, fp, fz, budget_s=20.0):
     t0 = time.perf_counter()
     CO.run(p, a, b, fp, fz, k, w["dt"], False, th)
     dt = time.perf_counter() - t0
-    return {"value": k / dt, "unit": UNIT, "cores": th, "kind": "port",
+    # one thread, one step (the reference's per-rank work without MPI)
+    t0 = time.perf_counter()
+    CO.run(p, a, b, fp, fz, 1, w["dt"], False, 1)
+    dt1 = time.perf_counter() - t0
+    return {"value": k / dt, "unit": UNIT, "cores": th, "kind": "port", "value_1thread": 1.0 / dt1,
             "sample": f"{k} RK4 steps at {n}^2 FP64 (after 1 untimed), C/OpenMP restatement of the "
-                      f"reference step (35 C2R + 8 R2C per step as in the reference), {th} threads, "
-                      "MPI ranks: 1 (threads instead of MPI)"}
+                      f"reference step (35 C2R + 8 R2C per step as in the reference), {th} threads; "
+                      "value_1thread: 1 step on 1 thread; MPI ranks: 1 (threads instead of MPI)"}
 
 
 def run_reference(args):
