@@ -305,9 +305,11 @@ int r2d3c_fp64_fma_peak(double* tflops);
 int r2d3c_dev_ptr(r2d3c_ctx* ctx, int which, void** ptr);
 /* The plan chosen when the context was created (the counterpart of FFTW's
    measured plans, fftp2D.f90:54-56): each launch-schedule variant of the
-   bracket pass and of the update pass that computes bit-identical results is
-   timed on this GPU and the fastest kept.  JSON text of the timings and the
-   choices, NUL-terminated in buf (R2D3C_EINVAL if len is too small). */
+   derivative pass, the bracket pass and the update pass that computes
+   bit-identical results (transform groups per CTA, field chunks, persistent
+   CTAs) is timed on this GPU and the fastest kept.  JSON text of the timings
+   and the choices, NUL-terminated in buf (R2D3C_EINVAL if len is too
+   small). */
 int r2d3c_plan_report(r2d3c_ctx* ctx, char* buf, int len);
 /* The context's CUDA stream (cudaStream_t). */
 int r2d3c_stream(r2d3c_ctx* ctx, void** stream);

@@ -319,7 +319,7 @@ class Context:
     def plan_report(self) -> dict:
         """The launch-schedule autotuner's timings and choice (r2d3c_plan_report)."""
         import json
-        buf = C.create_string_buffer(4096)
+        buf = C.create_string_buffer(16384)
         check(load().r2d3c_plan_report(self._h, buf, len(buf)), "plan_report")
         return json.loads(buf.value.decode())
 

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
@@ -870,8 +871,9 @@ class EngineT final : public IEngine {
       using C = CfgA<T, N>;
       auto k = k_passA<T, N>;
       const int groups = (gd_.M + NT - 1) / NT;
-      const dim3 grid((groups + C::G - 1) / C::G, nb);
-      k<<<grid, C::THREADS, C::SMEM, st_>>>(a, b, tf, gd_, tw_a_, batch());
+      const int g = ga_ ? ga_ : C::G;  // groups per CTA, field chunks: autotuned
+      const dim3 grid((groups + g - 1) / g, nb, fa_);
+      k<<<grid, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(a, b, tf, gd_, tw_a_, batch());
       post("k_passA");
     });
   }
@@ -899,8 +901,10 @@ class EngineT final : public IEngine {
       }
       if (!persistent) {  // one CTA (group) per row pair; the only form below n = 2048
         auto k = k_passB<T, N, CFL>;
-        const dim3 grid((N / NR + C::G - 1) / C::G, nb);
-        k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
+        const int g = gb_ ? gb_ : C::G;  // groups per CTA: autotuned
+        const dim3 grid((N / NR + g - 1) / g, nb);
+        k<<<grid, C::TPF * g, g * PassSmem<T, N>::GROUP_ELEMS * sizeof(cpx<T>), st_>>>(tf, pb, kxo, gd_, inv4, tw_,
+                                                                                      enc_base_, batch());
         post("k_passB");
       }
     });
@@ -928,8 +932,9 @@ class EngineT final : public IEngine {
       if (!persistent) {  // one CTA (group) per column pair
         auto k = k_passC<T, N>;
         const int groups = (gd_.M + NT - 1) / NT;
-        const dim3 grid((groups + C::G - 1) / C::G, nb);
-        k<<<grid, C::THREADS, PassSmem<T, N>::SMEM, st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ],
+        const int g = gc_ ? gc_ : C::G;  // groups per CTA: autotuned
+        const dim3 grid((groups + g - 1) / g, nb);
+        k<<<grid, C::TPF * g, g * PassSmem<T, N>::GROUP_ELEMS * sizeof(cpx<T>), st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ],
                                                            pbase_[P_FP], pbase_[P_FZ], c1out, c2out, gd_, d_sc_,
                                                            scal_base_, o, tw_, batch(), t5, t6);
         post("k_passC");
@@ -989,133 +994,207 @@ class EngineT final : public IEngine {
     });
   }
 
-  // Launch-schedule autotuner, run once when a full engine is created: the
-  // variants of pass B that compute bit-identical results (one CTA per row
-  // pair; persistent cp.async-staged CTAs, as many as are resident or half
-  // of that) are timed with CUDA events on this engine's own buffers (3
-  // launches after 2 untimed ones) and the fastest is kept.  The transform
-  // radices, which change the rounding, are fixed per n.
+  // Launch-schedule autotuner, run once when a full engine is created.  The
+  // launch shapes of passes A, B and C that compute bit-identical results
+  // are timed with CUDA events on this engine's own buffers (3 launches
+  // after 2 untimed ones) and the fastest of each pass is kept:
+  //   A: transform groups per CTA (the config's G down to 1) x field chunks
+  //      (the six fields in 1, 2, 3 or 6 CTAs);
+  //   B: one group per row pair, G down to 1 groups per CTA, or (n = 512 ..
+  //      4096 FP32) persistent cp.async-staged CTAs, as many as are resident
+  //      or half of that;
+  //   C: the same with column pairs.
+  // Small grids gain from spreading the work over more SMs (256^2: the
+  // config's groups fill 6 CTAs in pass A); large ones from full CTAs.  The
+  // transform radices, which change the rounding, are fixed per n.
+  template <typename F>
+  float time_launches(F&& launch) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+    for (int i = 0; i < 2; ++i) launch();
+    cuda_check(cudaEventRecord(e0, st_), "cudaEventRecord");
+    for (int i = 0; i < 3; ++i) launch();
+    cuda_check(cudaEventRecord(e1, st_), "cudaEventRecord");
+    cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    float ms = 0.f;
+    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return 1e3f * ms / 3.f;
+  }
+  // R2D3C_GROUPS="ga,fa,gb,gc" fixes the groups per CTA of passes A, B, C
+  // and pass A's field chunks (0 for a group count: the config's G)
+  static void forced_groups(int G_A, int G_B, int G_C, int out[4]) {
+    out[0] = out[2] = out[3] = -1;
+    out[1] = -1;
+    const char* e = std::getenv("R2D3C_GROUPS");
+    if (!e) return;
+    int v[4];
+    if (std::sscanf(e, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]) != 4)
+      throw Error(kEINVAL, "R2D3C_GROUPS must be ga,fa,gb,gc");
+    auto group_ok = [](int g, int G) { return g == 0 || (g >= 1 && g <= G && (g & (g - 1)) == 0); };
+    if (!group_ok(v[0], G_A) || !group_ok(v[2], G_B) || !group_ok(v[3], G_C) ||
+        !(v[1] == 1 || v[1] == 2 || v[1] == 3 || v[1] == 6))
+      throw Error(kEINVAL, "R2D3C_GROUPS: group counts must be 0 or a power of two up to G, field chunks 1, 2, 3 or 6");
+    for (int i = 0; i < 4; ++i) out[i] = v[i];
+  }
   void autotune() {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
-      if constexpr (kPipeB<T, N>) {
-        const int saved = launches_;
-        cuda_check(cudaMemsetAsync(tf_, 0, sizeof(cpx<T>) * 6 * (size_t)gd_.M * n_ * nb_, st_), "memset");
-        int sms = 0;
-        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
-        struct Cand {
-          int mode, grid;
-        };
-        std::vector<Cand> cands = {{0, 0}, {1, pipeb_ctas_}};
-        if (pipeb_ctas_ >= 2 * sms) cands.push_back({1, pipeb_ctas_ / 2});
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
-        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
-        cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+      constexpr int GA = CfgA<T, N>::G;
+      constexpr int GB = Cfg<T, N, PassNT<T, N>::value>::G;
+      const int saved = launches_;
+      int forced[4];
+      forced_groups(GA, GB, GB, forced);
+      int sms = 0;
+      cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
+      // ---- pass A (reads the state, writes the derivative planes)
+      cuda_check(cudaMemsetAsync(tf_, 0, sizeof(cpx<T>) * 6 * (size_t)gd_.M * n_ * nb_, st_), "memset");
+      tune_a_.clear();
+      {
         float best = 0.f;
-        Cand pick = cands[0];
+        TuneRec pick{GA, 1, 0.f};
+        for (int g = GA; g >= 1; g /= 2)
+          for (int f : {1, 2, 3, 6}) {
+            ga_ = g;
+            fa_ = f;
+            const float us = time_launches([&] { launch_passA(pbase_[P_PS], pbase_[P_VZ], tf_, nb_); });
+            tune_a_.push_back({g, f, us});
+            if (tune_a_.size() == 1 || us < best) {
+              best = us;
+              pick = tune_a_.back();
+            }
+          }
+        ga_ = forced[0] >= 0 ? (forced[0] ? forced[0] : GA) : pick.mode;
+        fa_ = forced[1] >= 0 ? forced[1] : pick.grid;
+      }
+      // ---- pass B (derivative planes -> bracket planes)
+      {
+        struct Cand {
+          int mode, grid, groups;
+        };
+        std::vector<Cand> cands;
+        for (int g = GB; g >= 1; g /= 2) cands.push_back({0, 0, g});
+        if constexpr (kPipeB<T, N>) {
+          cands.push_back({1, pipeb_ctas_, 0});
+          if (pipeb_ctas_ >= 2 * sms) cands.push_back({1, pipeb_ctas_ / 2, 0});
+        }
         tune_.clear();
+        float best = 0.f, best0 = 0.f;
+        size_t pick = 0, pick0 = 0;
         for (size_t ci = 0; ci < cands.size(); ++ci) {
           passb_mode_ = cands[ci].mode;
           pipeb_grid_ = cands[ci].grid;
-          for (int i = 0; i < 2; ++i) launch_passB<false>(gd_.M, tf_, pb_, nb_);
-          cuda_check(cudaEventRecord(e0, st_), "cudaEventRecord");
-          for (int i = 0; i < 3; ++i) launch_passB<false>(gd_.M, tf_, pb_, nb_);
-          cuda_check(cudaEventRecord(e1, st_), "cudaEventRecord");
-          cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
-          float ms = 0.f;
-          cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
-          const float us = 1e3f * ms / 3.f;
-          tune_.push_back({cands[ci].mode, cands[ci].grid, us});
-          if (ci == 0 || us < best) {
-            best = us;
-            pick = cands[ci];
-          }
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        // R2D3C_PASSB=per_row_pair|persistent overrides the measured choice
-        if (const char* force = std::getenv("R2D3C_PASSB")) {
-          if (std::strcmp(force, "per_row_pair") == 0) pick = cands[0];
-          else if (std::strcmp(force, "persistent") == 0) pick = cands[1];
-          else throw Error(kEINVAL, "R2D3C_PASSB must be per_row_pair or persistent");
-        }
-        passb_mode_ = pick.mode;
-        pipeb_grid_ = pick.grid;
-        launches_ = saved;
-      }
-      if constexpr (kPipeC<T, N>) {
-        // pass C on the engine's scratch planes (C1, C2 in and out), zero
-        // coefficients
-        const int saved = launches_;
-        cuda_check(cudaMemsetAsync(pb_, 0, sizeof(cpx<T>) * 2 * S_ * nb_, st_), "memset");
-        cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
-        int sms = 0;
-        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
-        std::vector<std::pair<int, int>> cands = {{0, 0}, {1, pipec_ctas_}};
-        if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2});
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
-        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
-        cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
-        float best = 0.f;
-        size_t pick = 0;
-        tune_c_.clear();
-        cpx<T>* c1 = planes_[P_C1];
-        cpx<T>* c2 = planes_[P_C2];
-        for (size_t ci = 0; ci < cands.size(); ++ci) {
-          passc_mode_ = cands[ci].first;
-          pipec_grid_ = cands[ci].second;
-          for (int i = 0; i < 2; ++i) launch_passC(c1, c2, c1, c2, 4, nb_);
-          cuda_check(cudaEventRecord(e0, st_), "cudaEventRecord");
-          for (int i = 0; i < 3; ++i) launch_passC(c1, c2, c1, c2, 4, nb_);
-          cuda_check(cudaEventRecord(e1, st_), "cudaEventRecord");
-          cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
-          float ms = 0.f;
-          cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
-          const float us = 1e3f * ms / 3.f;
-          tune_c_.push_back({cands[ci].first, cands[ci].second, us});
+          gb_ = cands[ci].groups;
+          const float us = time_launches([&] { launch_passB<false>(gd_.M, tf_, pb_, nb_); });
+          tune_.push_back({cands[ci].mode, cands[ci].mode ? cands[ci].grid : cands[ci].groups, us});
           if (ci == 0 || us < best) {
             best = us;
             pick = ci;
           }
+          if (cands[ci].mode == 0 && (ci == 0 || us < best0)) {
+            best0 = us;
+            pick0 = ci;
+          }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        // R2D3C_PASSB=per_row_pair|persistent overrides the measured choice
+        // (persistent where it exists: FP32, n = 512 .. 4096)
+        if (const char* force = std::getenv("R2D3C_PASSB")) {
+          if (std::strcmp(force, "per_row_pair") == 0) pick = pick0;
+          else if (std::strcmp(force, "persistent") == 0) pick = kPipeB<T, N> ? (size_t)(ilog2(GB) + 1) : pick0;
+          else throw Error(kEINVAL, "R2D3C_PASSB must be per_row_pair or persistent");
+        }
+        passb_mode_ = cands[pick].mode;
+        pipeb_grid_ = cands[pick].grid;
+        gb_ = forced[2] >= 0 ? (forced[2] ? forced[2] : GB) : cands[passb_mode_ ? pick0 : pick].groups;
+      }
+      // ---- pass C on the engine's scratch planes (C1, C2 in and out), zero
+      // coefficients
+      {
+        cuda_check(cudaMemsetAsync(pb_, 0, sizeof(cpx<T>) * 2 * S_ * nb_, st_), "memset");
+        cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
+        struct Cand {
+          int mode, grid, groups;
+        };
+        std::vector<Cand> cands;
+        for (int g = GB; g >= 1; g /= 2) cands.push_back({0, 0, g});
+        if constexpr (kPipeC<T, N>) {
+          cands.push_back({1, pipec_ctas_, 0});
+          if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2, 0});
+        }
+        tune_c_.clear();
+        float best = 0.f, best0 = 0.f;
+        size_t pick = 0, pick0 = 0;
+        cpx<T>* c1 = planes_[P_C1];
+        cpx<T>* c2 = planes_[P_C2];
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+          passc_mode_ = cands[ci].mode;
+          pipec_grid_ = cands[ci].grid;
+          gc_ = cands[ci].groups;
+          const float us = time_launches([&] { launch_passC(c1, c2, c1, c2, 4, nb_); });
+          tune_c_.push_back({cands[ci].mode, cands[ci].mode ? cands[ci].grid : cands[ci].groups, us});
+          if (ci == 0 || us < best) {
+            best = us;
+            pick = ci;
+          }
+          if (cands[ci].mode == 0 && (ci == 0 || us < best0)) {
+            best0 = us;
+            pick0 = ci;
+          }
+        }
         // R2D3C_PASSC=per_column_pair|persistent overrides the measured choice
+        // (persistent where it exists: FP32, n = 512 .. 4096)
         if (const char* force = std::getenv("R2D3C_PASSC")) {
-          if (std::strcmp(force, "per_column_pair") == 0) pick = 0;
-          else if (std::strcmp(force, "persistent") == 0) pick = 1;
+          if (std::strcmp(force, "per_column_pair") == 0) pick = pick0;
+          else if (std::strcmp(force, "persistent") == 0) pick = kPipeC<T, N> ? (size_t)(ilog2(GB) + 1) : pick0;
           else throw Error(kEINVAL, "R2D3C_PASSC must be per_column_pair or persistent");
         }
-        passc_mode_ = cands[pick].first;
-        pipec_grid_ = cands[pick].second;
+        passc_mode_ = cands[pick].mode;
+        pipec_grid_ = cands[pick].grid;
+        gc_ = forced[3] >= 0 ? (forced[3] ? forced[3] : GB) : cands[passc_mode_ ? pick0 : pick].groups;
         cuda_check(cudaMemsetAsync(planes_[P_C1], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
         cuda_check(cudaMemsetAsync(planes_[P_C2], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
-        launches_ = saved;
       }
+      launches_ = saved;
     });
   }
 
  public:
   std::string plan_report() const override {
-    std::string r = "{\"pass_b\": [";
-    for (size_t i = 0; i < tune_.size(); ++i) {
-      char b[160];
-      snprintf(b, sizeof b, "%s{\"variant\": \"%s\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
-               tune_[i].mode ? "persistent" : "per_row_pair", tune_[i].grid, (double)tune_[i].us);
+    std::string r = "{\"pass_a\": [";
+    char b[200];
+    for (size_t i = 0; i < tune_a_.size(); ++i) {
+      snprintf(b, sizeof b, "%s{\"groups\": %d, \"field_chunks\": %d, \"us\": %.2f}", i ? ", " : "",
+               tune_a_[i].mode, tune_a_[i].grid, (double)tune_a_[i].us);
       r += b;
     }
-    char b[160];
-    snprintf(b, sizeof b, "], \"chosen\": \"%s\", \"ctas\": %d", passb_mode_ ? "persistent" : "per_row_pair",
-             passb_mode_ ? pipeb_grid_ : 0);
+    snprintf(b, sizeof b, "], \"groups_a\": %d, \"field_chunks_a\": %d, \"pass_b\": [", ga_, fa_);
+    r += b;
+    for (size_t i = 0; i < tune_.size(); ++i) {
+      if (tune_[i].mode)
+        snprintf(b, sizeof b, "%s{\"variant\": \"persistent\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
+                 tune_[i].grid, (double)tune_[i].us);
+      else
+        snprintf(b, sizeof b, "%s{\"variant\": \"per_row_pair\", \"groups\": %d, \"us\": %.2f}", i ? ", " : "",
+                 tune_[i].grid, (double)tune_[i].us);
+      r += b;
+    }
+    snprintf(b, sizeof b, "], \"chosen\": \"%s\", \"ctas\": %d, \"groups_b\": %d",
+             passb_mode_ ? "persistent" : "per_row_pair", passb_mode_ ? pipeb_grid_ : 0, gb_);
     r += b;
     r += ", \"pass_c\": [";
     for (size_t i = 0; i < tune_c_.size(); ++i) {
-      snprintf(b, sizeof b, "%s{\"variant\": \"%s\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
-               tune_c_[i].mode ? "persistent" : "per_column_pair", tune_c_[i].grid, (double)tune_c_[i].us);
+      if (tune_c_[i].mode)
+        snprintf(b, sizeof b, "%s{\"variant\": \"persistent\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
+                 tune_c_[i].grid, (double)tune_c_[i].us);
+      else
+        snprintf(b, sizeof b, "%s{\"variant\": \"per_column_pair\", \"groups\": %d, \"us\": %.2f}", i ? ", " : "",
+                 tune_c_[i].grid, (double)tune_c_[i].us);
       r += b;
     }
-    snprintf(b, sizeof b, "], \"chosen_c\": \"%s\", \"ctas_c\": %d}",
-             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0);
+    snprintf(b, sizeof b, "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d}",
+             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_);
     return r + b;
   }
 
@@ -1153,11 +1232,13 @@ class EngineT final : public IEngine {
   int pipec_ctas_ = 0;  // resident CTAs of the persistent pass C (whole device)
   int passc_mode_ = 0;  // 0: one CTA per column pair, 1: persistent (autotuned)
   int pipec_grid_ = 0;  // CTAs of the persistent pass C (autotuned)
+  int ga_ = 0, fa_ = 1;  // pass A: groups per CTA (0: the config's G), field chunks (autotuned)
+  int gb_ = 0, gc_ = 0;  // passes B, C one CTA per row / column pair: groups per CTA (autotuned)
   struct TuneRec {
-    int mode, grid;
+    int mode, grid;  // pass A: groups, field chunks; B, C: variant, CTAs or groups
     float us;
   };
-  std::vector<TuneRec> tune_, tune_c_;
+  std::vector<TuneRec> tune_a_, tune_, tune_c_;
   cpx<T>* pbase_[P_COUNT] = {};
   double* scal_base_ = nullptr;
   unsigned long long* enc_base_ = nullptr;

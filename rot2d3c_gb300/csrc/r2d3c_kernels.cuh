@@ -303,7 +303,12 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
-  const int kx0 = (blockIdx.x * C::G + g) * NT;
+  // groups per CTA and field chunks are launch-time choices (blockDim.x =
+  // groups * TPF, gridDim.z chunks of the six fields): small grids spread
+  // one column pair's fields over several CTAs; the arithmetic per field is
+  // the same whatever the split
+  const int kx0 = (blockIdx.x * (blockDim.x / C::TPF) + g) * NT;
+  const int fpc = 6 / gridDim.z, f0 = blockIdx.z * fpc;
   const size_t plane = (size_t)gd.M * N;
   int kyi[C::E];
 #pragma unroll
@@ -318,10 +323,9 @@ k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __
     return in ? sp[(size_t)col * N + lane + q * C::TPF] : czero<T>();
   };
 #pragma unroll 1
-  for (int src = 0; src < 2; ++src) {  // psi for fields 0-3, vz for fields 4-5
-    const cpx<T>* sp = src == 0 ? ps : vz;
-#pragma unroll 1
-    for (int f = src * 4; f < (src == 0 ? 4 : 6); ++f) {
+  for (int f = f0; f < f0 + fpc; ++f) {
+    const cpx<T>* sp = f < 4 ? ps : vz;  // psi for fields 0-3, vz for fields 4-5
+    {
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
         const int col = kx0 + t;
@@ -455,7 +459,7 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
   cpx<T>* hold = sm + NR * F::SMEM_ELEMS;  // z1 store (HOLD)
-  int rg = blockIdx.x * C::G + g;
+  int rg = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
   const bool ok = rg < N / NR;
   if (!ok) rg = 0;  // surplus groups recompute rows 0.. and store nothing
   const int y0 = rg * NR;
@@ -957,7 +961,7 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   const int g = threadIdx.x / C::TPF, lane0 = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
   cpx<T>* hold = sm + NT * F::SMEM_ELEMS;  // transformed [psi,-k^2 psi] columns (HOLD)
-  const int kx0 = (blockIdx.x * C::G + g) * NT;
+  const int kx0 = (blockIdx.x * (blockDim.x / C::TPF) + g) * NT;  // groups per CTA: a launch-time choice
   const size_t oplane = (size_t)gd.nh * N;
   // The RK update at the end reads six spectral planes (eight with the
   // closure tendencies) on this group's columns; they are prefetched into L2

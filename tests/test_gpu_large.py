@@ -93,6 +93,7 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     c = gpu.Context(cp, 1)
     rep = c.plan_report()
     assert {r["variant"] for r in rep["pass_b"]} == {"per_row_pair", "persistent"}
+    assert rep["pass_a"] and all(r["us"] > 0 for r in rep["pass_a"])
     assert all(r["us"] > 0 for r in rep["pass_b"]) and rep["chosen"] in ("per_row_pair", "persistent")
     assert {r["variant"] for r in rep["pass_c"]} == {"per_column_pair", "persistent"}
     assert all(r["us"] > 0 for r in rep["pass_c"]) and rep["chosen_c"] in ("per_column_pair", "persistent")
@@ -112,5 +113,36 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     for u, v in zip(out[0], out[1]):
         np.testing.assert_array_equal(u, v)
     small = gpu.Context(params(64, iflow=0)[1], 1).plan_report()
-    assert small["pass_b"] == [] and small["chosen"] == "per_row_pair"
-    assert small["pass_c"] == [] and small["chosen_c"] == "per_column_pair"
+    assert {r["variant"] for r in small["pass_b"]} == {"per_row_pair"} and small["chosen"] == "per_row_pair"
+    assert {r["variant"] for r in small["pass_c"]} == {"per_column_pair"} and small["chosen_c"] == "per_column_pair"
+
+
+@pytest.mark.parametrize("n,prec", [(256, 1), (256, 0), (512, 1), (1024, 0)])
+def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
+    """Groups per CTA (passes A, B, C) and pass A's field chunks are launch
+    shapes only: every forced choice steps to the same bits as the tuned one."""
+    cp, ps, vz, fp, fz = _case(n, 5)
+    out, reps = [], []
+    for forced in (None, "1,6,1,1", "0,1,0,0", "2,3,1,2"):
+        if forced is None:
+            monkeypatch.delenv("R2D3C_GROUPS", raising=False)
+        else:
+            monkeypatch.setenv("R2D3C_GROUPS", forced)
+        monkeypatch.setenv("R2D3C_PASSB", "per_row_pair")
+        monkeypatch.setenv("R2D3C_PASSC", "per_column_pair")
+        c = gpu.Context(cp, prec)
+        reps.append(c.plan_report())
+        c.set_state(ps, vz)
+        c.set_forcing(fp, fz)
+        c.set_time(0.0)
+        c.advance(3, gpu.DT_CFL, 0.5)
+        out.append(c.get_state())
+        c.destroy()
+    assert reps[1]["groups_a"] == 1 and reps[1]["field_chunks_a"] == 6 and reps[1]["groups_b"] == 1
+    assert reps[3]["field_chunks_a"] == 3
+    for o in out[1:]:
+        for u, v in zip(out[0], o):
+            np.testing.assert_array_equal(u, v)
+    monkeypatch.setenv("R2D3C_GROUPS", "3,1,1,1")
+    with pytest.raises(gpu.R2D3CError):
+        gpu.Context(cp, prec)
