@@ -806,14 +806,17 @@ struct r2d3c_cnn {
     cuda_check(cudaGetLastError(), "k_conv_wgrad");
   }
 
-  // forward of a batch of B inputs (f32 NHWC 8 ch) -> pre[kLayers-1] (f32 NHWC 2 ch)
-  void forward(const float* x, int B) {
+  // forward of a batch of B inputs (f32 NHWC 8 ch) -> pre[kLayers-1] (f32 NHWC 2 ch);
+  // the hidden layers' pre-activations (kept for the backward pass) are
+  // written only when train is set
+  void forward(const float* x, int B, bool train) {
     const size_t npix = (size_t)B * H * W;
     k_to_bf16<<<1024, 256, 0, st>>>(x, npix, 8, 16, norm, norm + 8, act[0]);
     cuda_check(cudaGetLastError(), "k_to_bf16");
     for (int l = 0; l < kLayers; ++l) {
       const bool last = l == kLayers - 1;
-      conv(l, act[l], wf[l], B, pre[l], last ? nullptr : act[l + 1], last ? 0 : 1, true, false);
+      conv(l, act[l], wf[l], B, last || train ? pre[l] : nullptr, last ? nullptr : act[l + 1], last ? 0 : 1, true,
+           false);
     }
   }
 
@@ -882,7 +885,7 @@ void cnn_forward_on(r2d3c_cnn* c, const float* d_x, int batch, float* d_out, cud
   cudaStream_t own = c->st;
   c->st = stream;
   try {
-    c->forward(d_x, batch);
+    c->forward(d_x, batch, false);
     k_denorm<<<512, 256, 0, stream>>>(c->pre[kLayers - 1], (size_t)batch * c->H * c->W, c->norm + 16,
                                       c->norm + 18, d_out);
     cuda_check(cudaGetLastError(), "k_denorm");
@@ -1053,7 +1056,7 @@ int r2d3c_cnn_forward(r2d3c_cnn* c, const float* d_x, int batch, float* d_out) {
   try {
     if (!c || !d_x || !d_out) throw Error(kEINVAL, "NULL argument");
     if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
-    c->forward(d_x, batch);
+    c->forward(d_x, batch, false);
     k_denorm<<<512, 256, 0, c->st>>>(c->pre[kLayers - 1], (size_t)batch * c->H * c->W, c->norm + 16, c->norm + 18,
                                      d_out);
     cuda_check(cudaGetLastError(), "k_denorm");
@@ -1069,7 +1072,7 @@ int r2d3c_cnn_gradients(r2d3c_cnn* c, const float* d_x, const float* d_y, int ba
   try {
     if (!c || !d_x || !d_y) throw Error(kEINVAL, "NULL argument");
     if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
-    c->forward(d_x, batch);
+    c->forward(d_x, batch, true);
     const double l = c->backward(d_y, batch);
     c->check_err();
     if (loss) *loss = l;
@@ -1088,7 +1091,7 @@ int r2d3c_cnn_train_step(r2d3c_cnn* c, const float* d_x, const float* d_y, int b
   try {
     if (!c || !d_x || !d_y) throw Error(kEINVAL, "NULL argument");
     if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
-    c->forward(d_x, batch);
+    c->forward(d_x, batch, true);
     const double l = c->backward(d_y, batch);
     c->adam(lr);
     c->check_err();
