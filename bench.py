@@ -94,6 +94,14 @@ def synthetic_field(n, kmin, kmax, amp_slope, seed):
     return a, ka2
 
 
+def plan_summary(ctx):
+    """The launch shapes the plan autotuner chose for this context."""
+    r = ctx.plan_report()
+    return {"pass_a": {"groups": r["groups_a"], "field_chunks": r["field_chunks_a"]},
+            "pass_b": r["chosen"] if r["chosen"] == "persistent" else f"per_row_pair x{r['groups_b']}",
+            "pass_c": r["chosen_c"] if r["chosen_c"] == "persistent" else f"per_column_pair x{r['groups_c']}"}
+
+
 def workload_inputs(n):
     """(ps, vz, fp, fz) of the 4096^2 workload (scaled to n for smaller runs)."""
     import numpy as np
@@ -573,7 +581,8 @@ def main():
                                    "Omega=10, IC k^-3 1<=|k|<=100, forcing shell 20-22",
                        "n": n, "precision": "FP32 path (headline) and FP64 path (fp64)",
                        "l2": "working set larger than L2 (6 mixed planes of 268 MB at 4096^2 FP32)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "plan": plan_summary(c32)},
             "gpu_launches": launches32, "roofline": roofline, "clocks": clocks, "e2e": e2e,
             "fp64": fp64, "ensemble": ensemble, "closure": closure, "cpu_baseline": cpu}
     if rank == 0:

@@ -996,8 +996,8 @@ class EngineT final : public IEngine {
 
   // Launch-schedule autotuner, run once when a full engine is created.  The
   // launch shapes of passes A, B and C that compute bit-identical results
-  // are timed with CUDA events on this engine's own buffers (3 launches
-  // after 2 untimed ones) and the fastest of each pass is kept:
+  // are timed with CUDA events on this engine's own buffers (time_candidates)
+  // and the fastest of each pass is kept:
   //   A: transform groups per CTA (the config's G down to 1) x field chunks
   //      (the six fields in 1, 2, 3 or 6 CTAs);
   //   B: one group per row pair, G down to 1 groups per CTA, or (n = 512 ..
@@ -1007,21 +1007,30 @@ class EngineT final : public IEngine {
   // Small grids gain from spreading the work over more SMs (256^2: the
   // config's groups fill 6 CTAs in pass A); large ones from full CTAs.  The
   // transform radices, which change the rounding, are fixed per n.
-  template <typename F>
-  float time_launches(F&& launch) {
+  // Time per launch (us) of each of nc candidates: one untimed launch of
+  // every candidate, then three rounds over all of them (interleaved, so that
+  // clock or cache drift affects them alike), each round three launches of a
+  // candidate between two events; a candidate's fastest round counts.
+  std::vector<float> time_candidates(size_t nc, const std::function<void(size_t)>& launch) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
     cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
-    for (int i = 0; i < 2; ++i) launch();
-    cuda_check(cudaEventRecord(e0, st_), "cudaEventRecord");
-    for (int i = 0; i < 3; ++i) launch();
-    cuda_check(cudaEventRecord(e1, st_), "cudaEventRecord");
-    cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
-    float ms = 0.f;
-    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    std::vector<float> best(nc, 0.f);
+    for (size_t c = 0; c < nc; ++c) launch(c);
+    for (int round = 0; round < 3; ++round)
+      for (size_t c = 0; c < nc; ++c) {
+        cuda_check(cudaEventRecord(e0, st_), "cudaEventRecord");
+        for (int i = 0; i < 3; ++i) launch(c);
+        cuda_check(cudaEventRecord(e1, st_), "cudaEventRecord");
+        cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float ms = 0.f;
+        cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        const float us = 1e3f * ms / 3.f;
+        if (round == 0 || us < best[c]) best[c] = us;
+      }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return 1e3f * ms / 3.f;
+    return best;
   }
   // R2D3C_GROUPS="ga,fa,gb,gc" fixes the groups per CTA of passes A, B, C
   // and pass A's field chunks (0 for a group count: the config's G)
@@ -1049,55 +1058,51 @@ class EngineT final : public IEngine {
       forced_groups(GA, GB, GB, forced);
       int sms = 0;
       cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
+      auto argmin = [](const std::vector<float>& t, const std::function<bool(size_t)>& ok) {
+        size_t k = t.size();
+        for (size_t i = 0; i < t.size(); ++i)
+          if (ok(i) && (k == t.size() || t[i] < t[k])) k = i;
+        return k;
+      };
       // ---- pass A (reads the state, writes the derivative planes)
       cuda_check(cudaMemsetAsync(tf_, 0, sizeof(cpx<T>) * 6 * (size_t)gd_.M * n_ * nb_, st_), "memset");
-      tune_a_.clear();
       {
-        float best = 0.f;
-        TuneRec pick{GA, 1, 0.f};
+        std::vector<std::pair<int, int>> cands;  // (groups per CTA, field chunks)
         for (int g = GA; g >= 1; g /= 2)
-          for (int f : {1, 2, 3, 6}) {
-            ga_ = g;
-            fa_ = f;
-            const float us = time_launches([&] { launch_passA(pbase_[P_PS], pbase_[P_VZ], tf_, nb_); });
-            tune_a_.push_back({g, f, us});
-            if (tune_a_.size() == 1 || us < best) {
-              best = us;
-              pick = tune_a_.back();
-            }
-          }
-        ga_ = forced[0] >= 0 ? (forced[0] ? forced[0] : GA) : pick.mode;
-        fa_ = forced[1] >= 0 ? forced[1] : pick.grid;
+          for (int f : {1, 2, 3, 6}) cands.push_back({g, f});
+        const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
+          ga_ = cands[i].first;
+          fa_ = cands[i].second;
+          launch_passA(pbase_[P_PS], pbase_[P_VZ], tf_, nb_);
+        });
+        tune_a_.clear();
+        for (size_t i = 0; i < cands.size(); ++i) tune_a_.push_back({cands[i].first, cands[i].second, us[i]});
+        const size_t pick = argmin(us, [](size_t) { return true; });
+        ga_ = forced[0] >= 0 ? (forced[0] ? forced[0] : GA) : cands[pick].first;
+        fa_ = forced[1] >= 0 ? forced[1] : cands[pick].second;
       }
+      struct Cand {
+        int mode, grid, groups;  // mode 1: persistent with grid CTAs; mode 0: groups per CTA
+      };
       // ---- pass B (derivative planes -> bracket planes)
       {
-        struct Cand {
-          int mode, grid, groups;
-        };
         std::vector<Cand> cands;
         for (int g = GB; g >= 1; g /= 2) cands.push_back({0, 0, g});
         if constexpr (kPipeB<T, N>) {
           cands.push_back({1, pipeb_ctas_, 0});
           if (pipeb_ctas_ >= 2 * sms) cands.push_back({1, pipeb_ctas_ / 2, 0});
         }
+        const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
+          passb_mode_ = cands[i].mode;
+          pipeb_grid_ = cands[i].grid;
+          gb_ = cands[i].groups;
+          launch_passB<false>(gd_.M, tf_, pb_, nb_);
+        });
         tune_.clear();
-        float best = 0.f, best0 = 0.f;
-        size_t pick = 0, pick0 = 0;
-        for (size_t ci = 0; ci < cands.size(); ++ci) {
-          passb_mode_ = cands[ci].mode;
-          pipeb_grid_ = cands[ci].grid;
-          gb_ = cands[ci].groups;
-          const float us = time_launches([&] { launch_passB<false>(gd_.M, tf_, pb_, nb_); });
-          tune_.push_back({cands[ci].mode, cands[ci].mode ? cands[ci].grid : cands[ci].groups, us});
-          if (ci == 0 || us < best) {
-            best = us;
-            pick = ci;
-          }
-          if (cands[ci].mode == 0 && (ci == 0 || us < best0)) {
-            best0 = us;
-            pick0 = ci;
-          }
-        }
+        for (size_t i = 0; i < cands.size(); ++i)
+          tune_.push_back({cands[i].mode, cands[i].mode ? cands[i].grid : cands[i].groups, us[i]});
+        const size_t pick0 = argmin(us, [&](size_t i) { return cands[i].mode == 0; });
+        size_t pick = argmin(us, [](size_t) { return true; });
         // R2D3C_PASSB=per_row_pair|persistent overrides the measured choice
         // (persistent where it exists: FP32, n = 512 .. 4096)
         if (const char* force = std::getenv("R2D3C_PASSB")) {
@@ -1107,42 +1112,32 @@ class EngineT final : public IEngine {
         }
         passb_mode_ = cands[pick].mode;
         pipeb_grid_ = cands[pick].grid;
-        gb_ = forced[2] >= 0 ? (forced[2] ? forced[2] : GB) : cands[passb_mode_ ? pick0 : pick].groups;
+        gb_ = forced[2] >= 0 ? (forced[2] ? forced[2] : GB) : cands[pick0].groups;
       }
       // ---- pass C on the engine's scratch planes (C1, C2 in and out), zero
       // coefficients
       {
         cuda_check(cudaMemsetAsync(pb_, 0, sizeof(cpx<T>) * 2 * S_ * nb_, st_), "memset");
         cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
-        struct Cand {
-          int mode, grid, groups;
-        };
         std::vector<Cand> cands;
         for (int g = GB; g >= 1; g /= 2) cands.push_back({0, 0, g});
         if constexpr (kPipeC<T, N>) {
           cands.push_back({1, pipec_ctas_, 0});
           if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2, 0});
         }
-        tune_c_.clear();
-        float best = 0.f, best0 = 0.f;
-        size_t pick = 0, pick0 = 0;
         cpx<T>* c1 = planes_[P_C1];
         cpx<T>* c2 = planes_[P_C2];
-        for (size_t ci = 0; ci < cands.size(); ++ci) {
-          passc_mode_ = cands[ci].mode;
-          pipec_grid_ = cands[ci].grid;
-          gc_ = cands[ci].groups;
-          const float us = time_launches([&] { launch_passC(c1, c2, c1, c2, 4, nb_); });
-          tune_c_.push_back({cands[ci].mode, cands[ci].mode ? cands[ci].grid : cands[ci].groups, us});
-          if (ci == 0 || us < best) {
-            best = us;
-            pick = ci;
-          }
-          if (cands[ci].mode == 0 && (ci == 0 || us < best0)) {
-            best0 = us;
-            pick0 = ci;
-          }
-        }
+        const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
+          passc_mode_ = cands[i].mode;
+          pipec_grid_ = cands[i].grid;
+          gc_ = cands[i].groups;
+          launch_passC(c1, c2, c1, c2, 4, nb_);
+        });
+        tune_c_.clear();
+        for (size_t i = 0; i < cands.size(); ++i)
+          tune_c_.push_back({cands[i].mode, cands[i].mode ? cands[i].grid : cands[i].groups, us[i]});
+        const size_t pick0 = argmin(us, [&](size_t i) { return cands[i].mode == 0; });
+        size_t pick = argmin(us, [](size_t) { return true; });
         // R2D3C_PASSC=per_column_pair|persistent overrides the measured choice
         // (persistent where it exists: FP32, n = 512 .. 4096)
         if (const char* force = std::getenv("R2D3C_PASSC")) {
@@ -1152,7 +1147,7 @@ class EngineT final : public IEngine {
         }
         passc_mode_ = cands[pick].mode;
         pipec_grid_ = cands[pick].grid;
-        gc_ = forced[3] >= 0 ? (forced[3] ? forced[3] : GB) : cands[passc_mode_ ? pick0 : pick].groups;
+        gc_ = forced[3] >= 0 ? (forced[3] ? forced[3] : GB) : cands[pick0].groups;
         cuda_check(cudaMemsetAsync(planes_[P_C1], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
         cuda_check(cudaMemsetAsync(planes_[P_C2], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
       }
