@@ -96,7 +96,10 @@ def synthetic_field(n, kmin, kmax, amp_slope, seed):
 
 def plan_summary(ctx):
     """The launch shapes the plan autotuner chose for this context."""
-    r = ctx.plan_report()
+    return plan_summary_dict(ctx.plan_report())
+
+
+def plan_summary_dict(r):
     return {"pass_a": {"groups": r["groups_a"], "field_chunks": r["field_chunks_a"]},
             "pass_b": r["chosen"] if r["chosen"] == "persistent" else f"per_row_pair x{r['groups_b']}",
             "pass_c": r["chosen_c"] if r["chosen_c"] == "persistent" else f"per_column_pair x{r['groups_c']}"}
@@ -341,6 +344,7 @@ def run_ensemble(args, torch):
     out = {"value": len(runs) / el, "unit": f"runs/s ({K} RK4 steps per run)",
            "runs": len(runs), "groups": [list(g) for g in ENSEMBLE["groups"]], "steps_per_run": K,
            "seconds": el, "gpu_launches": ens.kernel_launches() - l0, "dtype": "f32 (FP64 reductions)",
+           "plan": {str(g["n"]): plan_summary_dict(g["plan"]) for g in ens.plan_report()},
            "budget_residual": {"median": float(np.median(resid)), "max": float(resid.max()),
                                "definition": "|mean(dE_tot/dt - (inj - diss))| / mean|inj| over 100 steps, "
                                              "cond_check every 10 steps"},

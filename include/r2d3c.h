@@ -197,6 +197,9 @@ int r2d3c_ensemble_set_time(r2d3c_ensemble* ens, int run, double time);
 int r2d3c_ensemble_cond_check(r2d3c_ensemble* ens, int run, double time, double out[30]);
 int r2d3c_ensemble_spectrum(r2d3c_ensemble* ens, int run, double* Ek, double* Ezk);
 int r2d3c_ensemble_kernel_launches(const r2d3c_ensemble* ens, long long* count);
+/* The plan of every size group (as r2d3c_plan_report): JSON list of
+   {"n", "runs", "plan"} objects, NUL-terminated in buf. */
+int r2d3c_ensemble_plan_report(const r2d3c_ensemble* ens, char* buf, int len);
 
 /* ---- Learned subgrid closure (no counterpart in the reference) --------- */
 /* A periodic CNN of six 3x3 convolutions, 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2

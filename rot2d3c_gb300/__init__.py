@@ -412,6 +412,13 @@ class Ensemble:
         check(load().r2d3c_ensemble_kernel_launches(self._h, C.byref(c)), "ensemble_kernel_launches")
         return c.value
 
+    def plan_report(self) -> list:
+        """The plan autotuner's timings and choices of every size group."""
+        import json
+        buf = C.create_string_buffer(65536)
+        check(load().r2d3c_ensemble_plan_report(self._h, buf, len(buf)), "ensemble_plan_report")
+        return json.loads(buf.value.decode())
+
     def destroy(self) -> None:
         if getattr(self, "_h", None):
             load().r2d3c_ensemble_destroy(self._h)

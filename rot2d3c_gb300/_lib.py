@@ -101,6 +101,7 @@ SIGNATURES = {
     "r2d3c_ensemble_cond_check": (C.c_int, [_P, C.c_int, C.c_double, _D]),
     "r2d3c_ensemble_spectrum": (C.c_int, [_P, C.c_int, _D, _D]),
     "r2d3c_ensemble_kernel_launches": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "r2d3c_ensemble_plan_report": (C.c_int, [_P, C.c_char_p, C.c_int]),
     "r2d3c_cnn_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_P)]),
     "r2d3c_cnn_destroy": (C.c_int, [_P]),
     "r2d3c_cnn_num_params": (C.c_int, [_P, C.POINTER(C.c_longlong)]),

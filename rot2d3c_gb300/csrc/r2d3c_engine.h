@@ -138,6 +138,10 @@ class IEngine {
   virtual int kernel_launches() const = 0;
   // JSON text of the launch-schedule autotuner's measurements and choices
   virtual std::string plan_report() const = 0;
+  // Re-derive the launch choices from the autotuner's timings: policy 0 the
+  // fastest of every candidate, 1 only full CTAs or persistent CTAs (for
+  // ensembles whose size groups run concurrently)
+  virtual void set_plan_policy(int policy) = 0;
   // Per-kernel device time of nsteps RK4 steps with the dt already set,
   // measured with CUDA events recorded on the engine stream around every
   // launch: ms[k] = total milliseconds, cnt[k] = launches, for k = 0 pass A,

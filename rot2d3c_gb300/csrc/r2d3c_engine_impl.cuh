@@ -1054,16 +1054,8 @@ class EngineT final : public IEngine {
       constexpr int GA = CfgA<T, N>::G;
       constexpr int GB = Cfg<T, N, PassNT<T, N>::value>::G;
       const int saved = launches_;
-      int forced[4];
-      forced_groups(GA, GB, GB, forced);
       int sms = 0;
       cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
-      auto argmin = [](const std::vector<float>& t, const std::function<bool(size_t)>& ok) {
-        size_t k = t.size();
-        for (size_t i = 0; i < t.size(); ++i)
-          if (ok(i) && (k == t.size() || t[i] < t[k])) k = i;
-        return k;
-      };
       // ---- pass A (reads the state, writes the derivative planes)
       cuda_check(cudaMemsetAsync(tf_, 0, sizeof(cpx<T>) * 6 * (size_t)gd_.M * n_ * nb_, st_), "memset");
       {
@@ -1077,87 +1069,117 @@ class EngineT final : public IEngine {
         });
         tune_a_.clear();
         for (size_t i = 0; i < cands.size(); ++i) tune_a_.push_back({cands[i].first, cands[i].second, us[i]});
-        const size_t pick = argmin(us, [](size_t) { return true; });
-        ga_ = forced[0] >= 0 ? (forced[0] ? forced[0] : GA) : cands[pick].first;
-        fa_ = forced[1] >= 0 ? forced[1] : cands[pick].second;
       }
-      struct Cand {
-        int mode, grid, groups;  // mode 1: persistent with grid CTAs; mode 0: groups per CTA
-      };
+      // (mode, grid): mode 0 one CTA per row / column pair with `grid` groups
+      // per CTA; mode 1 persistent with `grid` CTAs
       // ---- pass B (derivative planes -> bracket planes)
       {
-        std::vector<Cand> cands;
-        for (int g = GB; g >= 1; g /= 2) cands.push_back({0, 0, g});
+        std::vector<std::pair<int, int>> cands;
+        for (int g = GB; g >= 1; g /= 2) cands.push_back({0, g});
         if constexpr (kPipeB<T, N>) {
-          cands.push_back({1, pipeb_ctas_, 0});
-          if (pipeb_ctas_ >= 2 * sms) cands.push_back({1, pipeb_ctas_ / 2, 0});
+          cands.push_back({1, pipeb_ctas_});
+          if (pipeb_ctas_ >= 2 * sms) cands.push_back({1, pipeb_ctas_ / 2});
         }
         const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
-          passb_mode_ = cands[i].mode;
-          pipeb_grid_ = cands[i].grid;
-          gb_ = cands[i].groups;
+          passb_mode_ = cands[i].first;
+          pipeb_grid_ = cands[i].first ? cands[i].second : 0;
+          gb_ = cands[i].first ? GB : cands[i].second;
           launch_passB<false>(gd_.M, tf_, pb_, nb_);
         });
         tune_.clear();
-        for (size_t i = 0; i < cands.size(); ++i)
-          tune_.push_back({cands[i].mode, cands[i].mode ? cands[i].grid : cands[i].groups, us[i]});
-        const size_t pick0 = argmin(us, [&](size_t i) { return cands[i].mode == 0; });
-        size_t pick = argmin(us, [](size_t) { return true; });
-        // R2D3C_PASSB=per_row_pair|persistent overrides the measured choice
-        // (persistent where it exists: FP32, n = 512 .. 4096)
-        if (const char* force = std::getenv("R2D3C_PASSB")) {
-          if (std::strcmp(force, "per_row_pair") == 0) pick = pick0;
-          else if (std::strcmp(force, "persistent") == 0) pick = kPipeB<T, N> ? (size_t)(ilog2(GB) + 1) : pick0;
-          else throw Error(kEINVAL, "R2D3C_PASSB must be per_row_pair or persistent");
-        }
-        passb_mode_ = cands[pick].mode;
-        pipeb_grid_ = cands[pick].grid;
-        gb_ = forced[2] >= 0 ? (forced[2] ? forced[2] : GB) : cands[pick0].groups;
+        for (size_t i = 0; i < cands.size(); ++i) tune_.push_back({cands[i].first, cands[i].second, us[i]});
       }
       // ---- pass C on the engine's scratch planes (C1, C2 in and out), zero
       // coefficients
       {
         cuda_check(cudaMemsetAsync(pb_, 0, sizeof(cpx<T>) * 2 * S_ * nb_, st_), "memset");
         cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
-        std::vector<Cand> cands;
-        for (int g = GB; g >= 1; g /= 2) cands.push_back({0, 0, g});
+        std::vector<std::pair<int, int>> cands;
+        for (int g = GB; g >= 1; g /= 2) cands.push_back({0, g});
         if constexpr (kPipeC<T, N>) {
-          cands.push_back({1, pipec_ctas_, 0});
-          if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2, 0});
+          cands.push_back({1, pipec_ctas_});
+          if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2});
         }
         cpx<T>* c1 = planes_[P_C1];
         cpx<T>* c2 = planes_[P_C2];
         const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
-          passc_mode_ = cands[i].mode;
-          pipec_grid_ = cands[i].grid;
-          gc_ = cands[i].groups;
+          passc_mode_ = cands[i].first;
+          pipec_grid_ = cands[i].first ? cands[i].second : 0;
+          gc_ = cands[i].first ? GB : cands[i].second;
           launch_passC(c1, c2, c1, c2, 4, nb_);
         });
         tune_c_.clear();
-        for (size_t i = 0; i < cands.size(); ++i)
-          tune_c_.push_back({cands[i].mode, cands[i].mode ? cands[i].grid : cands[i].groups, us[i]});
-        const size_t pick0 = argmin(us, [&](size_t i) { return cands[i].mode == 0; });
-        size_t pick = argmin(us, [](size_t) { return true; });
-        // R2D3C_PASSC=per_column_pair|persistent overrides the measured choice
-        // (persistent where it exists: FP32, n = 512 .. 4096)
-        if (const char* force = std::getenv("R2D3C_PASSC")) {
-          if (std::strcmp(force, "per_column_pair") == 0) pick = pick0;
-          else if (std::strcmp(force, "persistent") == 0) pick = kPipeC<T, N> ? (size_t)(ilog2(GB) + 1) : pick0;
-          else throw Error(kEINVAL, "R2D3C_PASSC must be per_column_pair or persistent");
-        }
-        passc_mode_ = cands[pick].mode;
-        pipec_grid_ = cands[pick].grid;
-        gc_ = forced[3] >= 0 ? (forced[3] ? forced[3] : GB) : cands[pick0].groups;
+        for (size_t i = 0; i < cands.size(); ++i) tune_c_.push_back({cands[i].first, cands[i].second, us[i]});
         cuda_check(cudaMemsetAsync(planes_[P_C1], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
         cuda_check(cudaMemsetAsync(planes_[P_C2], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
       }
       launches_ = saved;
     });
+    choose_plan();
+  }
+
+  // The launch choices from the autotuner's timings.  Policy 0: the fastest
+  // candidate of each pass.  Policy 1 (ensembles of several size groups,
+  // whose graphs run the groups side by side, where a flood of small CTAs
+  // from one group measured slower than full ones): pass A with the
+  // config's groups per CTA and all six fields in one CTA, passes B and C
+  // with the config's groups per CTA or persistent.  The environment
+  // overrides (R2D3C_PASSB, R2D3C_PASSC, R2D3C_GROUPS) apply to both.
+  void choose_plan() {
+    if (tune_a_.empty()) return;
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      constexpr int GA = CfgA<T, N>::G;
+      constexpr int GB = Cfg<T, N, PassNT<T, N>::value>::G;
+      int forced[4];
+      forced_groups(GA, GB, GB, forced);
+      auto argmin = [](const std::vector<TuneRec>& t, const std::function<bool(const TuneRec&)>& ok) {
+        size_t k = t.size();
+        for (size_t i = 0; i < t.size(); ++i)
+          if (ok(t[i]) && (k == t.size() || t[i].us < t[k].us)) k = i;
+        return k;
+      };
+      const int pol = policy_;
+      const size_t ka = argmin(tune_a_, [&](const TuneRec& r) { return pol == 0 || (r.mode == GA && r.grid == 1); });
+      ga_ = forced[0] >= 0 ? (forced[0] ? forced[0] : GA) : tune_a_[ka].mode;
+      fa_ = forced[1] >= 0 ? forced[1] : tune_a_[ka].grid;
+      auto pick_bc = [&](const std::vector<TuneRec>& t, const char* env, const char* pair_name, int forced_g,
+                         int& mode, int& grid, int& groups) {
+        auto ok = [&](const TuneRec& r) { return pol == 0 || r.mode == 1 || r.grid == GB; };
+        const size_t pick0 = argmin(t, [&](const TuneRec& r) { return r.mode == 0 && ok(r); });
+        size_t pick = argmin(t, ok);
+        // env=<pair_name>|persistent overrides the measured choice
+        // (persistent where it exists: FP32, n = 512 .. 4096)
+        if (const char* force = std::getenv(env)) {
+          if (std::strcmp(force, pair_name) == 0) {
+            pick = pick0;
+          } else if (std::strcmp(force, "persistent") == 0) {
+            // the first persistent candidate: all resident CTAs
+            size_t k = t.size();
+            for (size_t i = t.size(); i-- > 0;)
+              if (t[i].mode == 1) k = i;
+            pick = k < t.size() ? k : pick0;
+          } else {
+            throw Error(kEINVAL, std::string(env) + " must be " + pair_name + " or persistent");
+          }
+        }
+        mode = t[pick].mode;
+        grid = mode ? t[pick].grid : 0;
+        groups = forced_g >= 0 ? (forced_g ? forced_g : GB) : t[pick0].grid;
+      };
+      pick_bc(tune_, "R2D3C_PASSB", "per_row_pair", forced[2], passb_mode_, pipeb_grid_, gb_);
+      pick_bc(tune_c_, "R2D3C_PASSC", "per_column_pair", forced[3], passc_mode_, pipec_grid_, gc_);
+    });
+  }
+  void set_plan_policy(int policy) override {
+    if (policy != 0 && policy != 1) throw Error(kEINVAL, "plan policy must be 0 or 1");
+    policy_ = policy;
+    choose_plan();
   }
 
  public:
   std::string plan_report() const override {
-    std::string r = "{\"pass_a\": [";
+    std::string r = "{\"policy\": " + std::to_string(policy_) + ", \"pass_a\": [";
     char b[200];
     for (size_t i = 0; i < tune_a_.size(); ++i) {
       snprintf(b, sizeof b, "%s{\"groups\": %d, \"field_chunks\": %d, \"us\": %.2f}", i ? ", " : "",
@@ -1227,6 +1249,7 @@ class EngineT final : public IEngine {
   int pipec_ctas_ = 0;  // resident CTAs of the persistent pass C (whole device)
   int passc_mode_ = 0;  // 0: one CTA per column pair, 1: persistent (autotuned)
   int pipec_grid_ = 0;  // CTAs of the persistent pass C (autotuned)
+  int policy_ = 0;      // plan policy (choose_plan)
   int ga_ = 0, fa_ = 1;  // pass A: groups per CTA (0: the config's G), field chunks (autotuned)
   int gb_ = 0, gc_ = 0;  // passes B, C one CTA per row / column pair: groups per CTA (autotuned)
   struct TuneRec {

@@ -33,6 +33,9 @@ def test_ensemble_runs_equal_single_runs(gpu, prec, mode, val):
     times = ens.advance(4, mode, val)
     times = ens.advance(3, mode, val)
     assert ens.kernel_launches() > 0
+    plans = ens.plan_report()
+    assert [(p["n"], p["runs"]) for p in plans] == [(32, 3), (64, 2)]
+    assert all(p["plan"]["pass_a"] and p["plan"]["groups_a"] >= 1 for p in plans)
     for r, (n, cp, ps, vz, fp, fz) in enumerate(spec):
         c = gpu.Context(cp, prec)
         c.set_state(ps, vz)
