@@ -79,6 +79,7 @@ class EngineT final : public IEngine {
     if (nb < 1 || (nb > 1 && !full)) throw Error(kEINVAL, "bad batch size");
     if (!supported_n(n)) throw Error(kEINVAL, "unsupported grid size n");
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    cuda_check(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
     cuda_check(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking), "cudaStreamCreate");
     gd_.n = n;
     gd_.nh = n / 2 + 1;
@@ -822,13 +823,23 @@ class EngineT final : public IEngine {
   }
 
   // ---------------------------------------------------------------- launchers
+  // Groups per CTA of a generic transform launch over `units` transforms:
+  // the config's G, halved while the grid would have fewer than two CTAs per
+  // SM (on small grids more, smaller CTAs spread the transforms over the SMs;
+  // the results are the same)
+  int fft_groups(long long units, int G) const {
+    int g = G;
+    while (g > 1 && (units + g - 1) / g < 2LL * sms_) g /= 2;
+    return g;
+  }
   template <int DIR>
   void launch_colfft(const cpx<T>* in, cpx<T>* out, int ncols) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       using C = Cfg<T, N>;
       auto k = k_colfft<T, N, DIR>;
-      k<<<(ncols + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(in, out, ncols, tw_, 0);
+      const int g = fft_groups(ncols, C::G);
+      k<<<(ncols + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(in, out, ncols, tw_, 0);
       post("k_colfft");
     });
   }
@@ -840,7 +851,8 @@ class EngineT final : public IEngine {
       constexpr int PY = PassNT<T, N>::value;
       using C = Cfg<T, N>;
       auto k = k_colfft<T, N, -1, PY>;
-      k<<<(gd_.nh + C::G - 1) / C::G, C::THREADS, C::SMEM, st_>>>(in, out, gd_.nh, tw_, gd_.nh);
+      const int g = fft_groups(gd_.nh, C::G);
+      k<<<(gd_.nh + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(in, out, gd_.nh, tw_, gd_.nh);
       post("k_colfft");
     });
   }
@@ -850,7 +862,8 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       using C = Cfg<T, N>;
       auto k = k_rowc2r<T, N>;
-      k<<<dim3((N / 2 + C::G - 1) / C::G, nplanes), C::THREADS, C::SMEM, st_>>>(tin, rout, mm, tw_);
+      const int g = fft_groups((long long)(N / 2) * nplanes, C::G);
+      k<<<dim3((N / 2 + g - 1) / g, nplanes), C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(tin, rout, mm, tw_);
       post("k_rowc2r");
     });
   }
@@ -859,7 +872,8 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       using C = Cfg<T, N>;
       auto k = k_rowr2c<T, N>;
-      k<<<dim3((N / 2 + C::G - 1) / C::G, nplanes), C::THREADS, C::SMEM, st_>>>(rin, tout, tw_);
+      const int g = fft_groups((long long)(N / 2) * nplanes, C::G);
+      k<<<dim3((N / 2 + g - 1) / g, nplanes), C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(rin, tout, tw_);
       post("k_rowr2c");
     });
   }
@@ -1249,6 +1263,7 @@ class EngineT final : public IEngine {
   int pipec_ctas_ = 0;  // resident CTAs of the persistent pass C (whole device)
   int passc_mode_ = 0;  // 0: one CTA per column pair, 1: persistent (autotuned)
   int pipec_grid_ = 0;  // CTAs of the persistent pass C (autotuned)
+  int sms_ = 0;         // SMs of the device
   int policy_ = 0;      // plan policy (choose_plan)
   int ga_ = 0, fa_ = 1;  // pass A: groups per CTA (0: the config's G), field chunks (autotuned)
   int gb_ = 0, gc_ = 0;  // passes B, C one CTA per row / column pair: groups per CTA (autotuned)

@@ -163,7 +163,7 @@ k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* _
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
-  const int col = blockIdx.x * C::G + g;
+  const int col = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
   const bool ok = col < ncols;
   cpx<T> v[1][C::E];
 #pragma unroll
@@ -196,7 +196,7 @@ k_rowc2r(const cpx<T>* __restrict__ tin, T* __restrict__ rout,
   if (rout) rout += blockIdx.y * (size_t)N * N;
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
-  int pair = blockIdx.x * C::G + g;
+  int pair = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
   const bool ok = pair < N / 2;
   if (!ok) pair = 0;  // surplus groups recompute pair 0 and store nothing
   const int y0 = 2 * pair;
@@ -259,7 +259,7 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
   tout += blockIdx.y * (size_t)(N / 2 + 1) * N;
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
-  int pair = blockIdx.x * C::G + g;
+  int pair = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
   const bool ok = pair < N / 2;
   if (!ok) pair = 0;
   const int y0 = 2 * pair;
