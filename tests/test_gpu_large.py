@@ -84,7 +84,7 @@ def test_fp32_vs_fp64_at_8192_spectra(gpu):
     assert np.max(np.abs(ek32[live] - ek64[live]) / ek64[live]) < 1e-3
 
 
-@pytest.mark.parametrize("n", [512, 1024, 4096])
+@pytest.mark.parametrize("n", [512, 1024, 2048, 4096])
 def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     """The plan autotuner times the pass-B launch schedules at context
     creation; both schedules give bit-identical steps, so the choice never
@@ -99,7 +99,8 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     assert all(r["us"] > 0 for r in rep["pass_c"]) and rep["chosen_c"] in ("per_column_pair", "persistent")
     c.destroy()
     out = []
-    for mb, mc in (("per_row_pair", "per_column_pair"), ("persistent", "persistent")):
+    for mb, mc in (("per_row_pair", "per_column_pair"), ("persistent", "persistent"),
+                   ("persistent", "per_column_pair")):
         monkeypatch.setenv("R2D3C_PASSB", mb)
         monkeypatch.setenv("R2D3C_PASSC", mc)
         c = gpu.Context(cp, 1)
@@ -110,8 +111,9 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
         c.advance(2, gpu.DT_CFL, 0.5)
         out.append(c.get_state())
         c.destroy()
-    for u, v in zip(out[0], out[1]):
-        np.testing.assert_array_equal(u, v)
+    for o in out[1:]:
+        for u, v in zip(out[0], o):
+            np.testing.assert_array_equal(u, v)
     small = gpu.Context(params(64, iflow=0)[1], 1).plan_report()
     assert {r["variant"] for r in small["pass_b"]} == {"per_row_pair"} and small["chosen"] == "per_row_pair"
     assert {r["variant"] for r in small["pass_c"]} == {"per_column_pair"} and small["chosen_c"] == "per_column_pair"
