@@ -101,6 +101,8 @@ namespace r2d3c {
 void cnn_forward_on(r2d3c_cnn* c, const float* d_x, int batch, float* d_out, cudaStream_t stream);
 void cnn_shape(const r2d3c_cnn* c, int* H, int* W, int* max_batch, unsigned long long* serial);
 void cnn_check_err(r2d3c_cnn* c);
+void cnn_io(r2d3c_cnn* c, void** act0, const float** out, const float** norm);
+void cnn_layers_on(r2d3c_cnn* c, int batch, cudaStream_t stream);
 }  // namespace r2d3c
 
 struct r2d3c_plan {
@@ -1142,13 +1144,29 @@ int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mod
   e->set_closure(ctx->cl_t, true);  // closure on; the hook refreshes the tendencies before every step
   float* x = ctx->cl_x;
   float* t = ctx->cl_t;
-  e->set_step_hook(
-      [e, cnn, x, t](cudaStream_t s) {
-        e->closure_inputs(x, false);
-        cnn_forward_on(cnn, x, 1, t, s);
-        e->set_closure(t, false);
-      },
-      serial);
+  if (e->closure_fused()) {
+    // inputs straight into the network's first activation, tendencies
+    // straight from its output: two conversion kernels fewer on each side
+    void* act0 = nullptr;
+    const float* out = nullptr;
+    const float* norm = nullptr;
+    cnn_io(cnn, &act0, &out, &norm);
+    e->set_step_hook(
+        [e, cnn, act0, out, norm](cudaStream_t s) {
+          e->closure_inputs_cnn(act0, norm, norm + 8);
+          cnn_layers_on(cnn, 1, s);
+          e->set_closure_cnn(out, norm + 16, norm + 18);
+        },
+        serial);
+  } else {
+    e->set_step_hook(
+        [e, cnn, x, t](cudaStream_t s) {
+          e->closure_inputs(x, false);
+          cnn_forward_on(cnn, x, 1, t, s);
+          e->set_closure(t, false);
+        },
+        serial);
+  }
   try {
     if (dt_mode == R2D3C_DT_FIXED) e->set_dt(cfl_or_dt);
     e->advance(ctx->mc(), nsteps, dt_mode == R2D3C_DT_CFL, cfl_or_dt, nullptr);

@@ -2,6 +2,8 @@
 // initial-condition kernels of the Rot2D3C hot path (sm_103a).
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "r2d3c_kernels.cuh"
 
 namespace r2d3c {
@@ -524,34 +526,60 @@ __global__ void k_to_channel(const T* __restrict__ r, size_t count, double s, fl
     out[p * nch + ch] = (float)((double)r[p] * s);
 }
 
-// The 8 spectral fields of the closure's inputs from psi and vz in one pass
-// (the specop chain of closure_inputs, same arithmetic): planes c = 0..7 of
-// w8 (S elements each) = -k^2 psi, vz, d_x psi, d_y psi, d_x(-k^2 psi),
-// d_y(-k^2 psi), d_x vz, d_y vz; every field but the first masked to
-// k^2 <= kmax (the first is psi's own truncation).
+// Spectral field c (0..7) of the closure's inputs at (kx, ky) from psi (x)
+// and vz (z) (the specop chain of closure_inputs, same arithmetic):
+// -k^2 psi, vz, d_x psi, d_y psi, d_x(-k^2 psi), d_y(-k^2 psi), d_x vz,
+// d_y vz; every field but the first masked to k^2 <= kmax (the first is
+// psi's own truncation).
 template <typename T>
-__global__ void k_closure_specs(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, DevGrid gd,
-                                cpx<T>* __restrict__ w8) {
-  const size_t total = (size_t)gd.nh * gd.n;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
-    const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
-    const int k2 = kx * kx + ky * ky;
-    const bool in = k2 <= gd.kmaxi;
-    const cpx<T> x = ps[idx], z = vz[idx];
-    const T m = -(T)k2;
-    const cpx<T> L = mkc<T>(m * x.x, m * x.y);
-    const T fx = (T)kx, fy = (T)ky;
-    const cpx<T> zero = czero<T>();
-    w8[idx] = L;
-    w8[total + idx] = in ? z : zero;
-    w8[2 * total + idx] = in ? mkc<T>(-fx * x.y, fx * x.x) : zero;
-    w8[3 * total + idx] = in ? mkc<T>(-fy * x.y, fy * x.x) : zero;
-    w8[4 * total + idx] = in ? mkc<T>(-fx * L.y, fx * L.x) : zero;
-    w8[5 * total + idx] = in ? mkc<T>(-fy * L.y, fy * L.x) : zero;
-    w8[6 * total + idx] = in ? mkc<T>(-fx * z.y, fx * z.x) : zero;
-    w8[7 * total + idx] = in ? mkc<T>(-fy * z.y, fy * z.x) : zero;
+__device__ __forceinline__ cpx<T> closure_field(int c, cpx<T> x, cpx<T> z, int kx, int ky, int kmaxi) {
+  const int k2 = kx * kx + ky * ky;
+  const bool in = k2 <= kmaxi;
+  const T m = -(T)k2;
+  const cpx<T> L = mkc<T>(m * x.x, m * x.y);
+  const T fx = (T)kx, fy = (T)ky;
+  const cpx<T> zero = czero<T>();
+  switch (c) {
+    case 0: return L;
+    case 1: return in ? z : zero;
+    case 2: return in ? mkc<T>(-fx * x.y, fx * x.x) : zero;
+    case 3: return in ? mkc<T>(-fy * x.y, fy * x.x) : zero;
+    case 4: return in ? mkc<T>(-fx * L.y, fx * L.x) : zero;
+    case 5: return in ? mkc<T>(-fy * L.y, fy * L.x) : zero;
+    case 6: return in ? mkc<T>(-fx * z.y, fx * z.x) : zero;
+    default: return in ? mkc<T>(-fy * z.y, fy * z.x) : zero;
+  }
+}
+
+// The 8 closure-input fields and their inverse y-transforms in one kernel:
+// column col of the 8 * nh output columns (field col / nh, kx index
+// col % nh) is formed from psi and vz as it is loaded and transformed as
+// k_colfft does (out: 8 mixed planes [kx][y], one after the other).
+template <typename T, int N>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_closure_cols(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, DevGrid gd, cpx<T>* __restrict__ out,
+               const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
+  const int col = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
+  const bool ok = col < 8 * gd.nh;
+  const int c = ok ? col / gd.nh : 0, i = ok ? col % gd.nh : 0;
+  const int kx = kx_of(i, N);
+  cpx<T> v[1][C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int j = lane + q * C::TPF;
+    const size_t idx = (size_t)i * N + j;
+    v[0][q] = ok ? closure_field<T>(c, ps[idx], vz[idx], kx, ky_of(j, N), gd.kmaxi) : czero<T>();
+  }
+  F::template run<+1>(v, lane, sm, tw);
+  if (ok) {
+    cpx<T>* dst = out + (size_t)col * N;
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[0][q];
   }
 }
 
@@ -574,6 +602,122 @@ __global__ void k_from_channels2(const float* __restrict__ in, size_t count, T* 
     const float2 v = reinterpret_cast<const float2*>(in)[p];
     r2[p] = (T)v.x;
     r2[count + p] = (T)v.y;
+  }
+}
+
+// Fused closure path of the LES step (n <= 512).
+//
+// k_rows_to_cnn8: the row C2R of the 8 closure-input planes of row pair y0
+// (one transform group per plane, as k_rowc2r), then per pixel of the two
+// rows the 8 channel values scaled by s (k_to_channels8) and standardised
+// and rounded to bf16 (the network's input conversion), written as the 16
+// bf16 channels (8 zero) of the network's first activation: 32 bytes per
+// pixel.  Same arithmetic, in the same order, as the three separate kernels.
+template <typename T, int N>
+struct RowsCnn {
+  using C = Cfg<T, N>;
+  static constexpr int THREADS = 8 * C::TPF;
+  static constexpr size_t SMEM = 8 * C::FFT::SMEM_BYTES;
+  static constexpr bool OK = N <= 512 && THREADS <= 1024 && (size_t)C::FFT::SMEM_ELEMS * 2 >= (size_t)2 * N;
+};
+template <typename T, int N>
+__global__ void __launch_bounds__(RowsCnn<T, N>::THREADS)
+k_rows_to_cnn8(const cpx<T>* __restrict__ tin, Scale8 s, const float* __restrict__ mean,
+               const float* __restrict__ sd, __nv_bfloat16* __restrict__ act, const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;  // g: channel plane
+  cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
+  const cpx<T>* in = tin + (size_t)g * (N / 2 + 1) * N;
+  const int y0 = 2 * blockIdx.x;
+  cpx<T> v[1][C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int k = lane + q * C::TPF;
+    const int kk = k <= N / 2 ? k : N - k;
+    const cpx<T> a = in[(size_t)kk * N + y0];
+    const cpx<T> b = in[(size_t)kk * N + y0 + 1];
+    if (k == 0 || k == N / 2) {
+      v[0][q] = mkc<T>(a.x, b.x);
+    } else if (k < N / 2) {
+      v[0][q] = mkc<T>(a.x - b.y, a.y + b.x);
+    } else {
+      v[0][q] = mkc<T>(a.x + b.y, b.x - a.y);
+    }
+  }
+  F::template run<+1>(v, lane, sm, tw);
+  __syncthreads();  // every group's transform is done with its buffer
+  T* rows = reinterpret_cast<T*>(sm);  // this plane's rows y0, y0 + 1: [2][N]
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    rows[lane + q * C::TPF] = v[0][q].x;
+    rows[N + lane + q * C::TPF] = v[0][q].y;
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < 2 * N; p += blockDim.x) {
+    unsigned u[8];
+#pragma unroll
+    for (int c = 0; c < 8; c += 2) {
+      float o[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const T val = reinterpret_cast<const T*>(smbase_ + (size_t)(c + h) * F::SMEM_ELEMS)[p];
+        const float x = (float)((double)val * s.v[c + h]);
+        o[h] = (x - mean[c + h]) / sd[c + h];
+      }
+      const __nv_bfloat162 b2 = __floats2bfloat162_rn(o[0], o[1]);
+      u[c / 2] = *reinterpret_cast<const unsigned*>(&b2);
+    }
+    u[4] = u[5] = u[6] = u[7] = 0u;  // channels 8-15: padding
+    uint4* dst = reinterpret_cast<uint4*>(act + ((size_t)(y0 + p / N) * N + p % N) * 16);
+    dst[0] = make_uint4(u[0], u[1], u[2], u[3]);
+    dst[1] = make_uint4(u[4], u[5], u[6], u[7]);
+  }
+}
+
+// k_cnn2_to_rows: the network's output (standardised, FP32 NHWC, 2
+// channels; blockIdx.y = channel) de-standardised as the network's own
+// output conversion does (y * sd + mean, one fused multiply-add), as the two
+// rows of row pair y0 of that channel's tendency plane, then the row R2C of
+// k_rowr2c: k_denorm + k_from_channels2 + k_rowr2c in one kernel.
+template <typename T, int N>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_cnn2_to_rows(const float* __restrict__ y, const float* __restrict__ mean, const float* __restrict__ sd,
+               cpx<T>* __restrict__ tout, const tw_t<T>* __restrict__ tw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int ch = blockIdx.y;
+  tout += ch * (size_t)(N / 2 + 1) * N;
+  const float m = mean[ch], d = sd[ch];
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
+  int pair = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
+  const bool ok = pair < N / 2;
+  if (!ok) pair = 0;
+  const int y0 = 2 * pair;
+  cpx<T> v[1][C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int x = lane + q * C::TPF;
+    const T a = (T)fmaf(y[((size_t)y0 * N + x) * 2 + ch], d, m);
+    const T b = (T)fmaf(y[((size_t)(y0 + 1) * N + x) * 2 + ch], d, m);
+    v[0][q] = mkc<T>(a, b);
+  }
+  F::template run<-1>(v, lane, sm, tw);
+  F::to_smem(v, lane, sm);
+  fft_sync<C::TPF>();
+  const T h = (T)0.5;
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int k = lane + q * C::TPF;
+    if (ok && k <= N / 2) {
+      const cpx<T> w = F::from_smem(0, k, sm);
+      const cpx<T> u = F::from_smem(0, (N - k) & (N - 1), sm);
+      tout[(size_t)k * N + y0] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
+      tout[(size_t)k * N + y0 + 1] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+    }
   }
 }
 

@@ -659,12 +659,13 @@ __global__ void k_to_bf16(const float* __restrict__ x, size_t npix, int c, int c
   }
 }
 
-// out = y * std[ch] + mean[ch] for the 2 output channels
+// out = y * std[ch] + mean[ch] for the 2 output channels (one fused
+// multiply-add, as the fused closure path computes it)
 __global__ void k_denorm(const float* __restrict__ y, size_t npix, const float* __restrict__ mean,
                          const float* __restrict__ sd, float* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix * 2; i += (size_t)gridDim.x * blockDim.x) {
     const int ch = (int)(i & 1);
-    out[i] = y[i] * sd[ch] + mean[ch];
+    out[i] = fmaf(y[i], sd[ch], mean[ch]);
   }
 }
 
@@ -813,6 +814,10 @@ struct r2d3c_cnn {
     const size_t npix = (size_t)B * H * W;
     k_to_bf16<<<1024, 256, 0, st>>>(x, npix, 8, 16, norm, norm + 8, act[0]);
     cuda_check(cudaGetLastError(), "k_to_bf16");
+    layers(B, train);
+  }
+  // the six layers from act[0] (bf16, 16 ch) into pre[kLayers-1]
+  void layers(int B, bool train) {
     for (int l = 0; l < kLayers; ++l) {
       const bool last = l == kLayers - 1;
       conv(l, act[l], wf[l], B, last || train ? pre[l] : nullptr, last ? nullptr : act[l + 1], last ? 0 : 1, true,
@@ -896,6 +901,28 @@ void cnn_forward_on(r2d3c_cnn* c, const float* d_x, int batch, float* d_out, cud
   c->st = own;
 }
 void cnn_check_err(r2d3c_cnn* c) { c->check_err(); }
+// The network's input activation (bf16 [H][W][16] of batch entry 0), its
+// standardised output (f32 [H][W][2]) and its normalisation (in mean[8],
+// in std[8], out mean[2], out std[2]), for callers that fill the input and
+// read the output themselves (the fused LES step)
+void cnn_io(r2d3c_cnn* c, void** act0, const float** out, const float** norm) {
+  *act0 = c->act[0];
+  *out = c->pre[kLayers - 1];
+  *norm = c->norm;
+}
+// The six layers of a batch whose input activation is already in place,
+// queued on `stream` (capturable)
+void cnn_layers_on(r2d3c_cnn* c, int batch, cudaStream_t stream) {
+  cudaStream_t own = c->st;
+  c->st = stream;
+  try {
+    c->layers(batch, false);
+  } catch (...) {
+    c->st = own;
+    throw;
+  }
+  c->st = own;
+}
 void cnn_shape(const r2d3c_cnn* c, int* H, int* W, int* max_batch, unsigned long long* serial) {
   *H = c->H;
   *W = c->W;

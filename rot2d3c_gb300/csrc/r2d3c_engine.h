@@ -106,6 +106,15 @@ class IEngine {
   // following steps (physical FP32 [n][n][2]; null switches them off)
   // (wait = false: queue the work and return, for capture into a graph)
   virtual void closure_inputs(float* d_x, bool wait) = 0;
+  // Fused forms for the captured LES step (where closure_fused() is true):
+  // the inputs straight into the network's bf16 first activation
+  // ([n][n][16], standardised with in_mean/in_sd), and the tendencies
+  // straight from the network's standardised output ([n][n][2] FP32, with
+  // out_mean/out_sd); the same results as closure_inputs / set_closure with
+  // the network's own conversions
+  virtual bool closure_fused() const = 0;
+  virtual void closure_inputs_cnn(void* act0, const float* in_mean, const float* in_sd) = 0;
+  virtual void set_closure_cnn(const float* y, const float* out_mean, const float* out_sd) = 0;
   virtual void brackets() = 0;  // [psi,-k^2 psi] -> P_B5, [psi,vz] -> P_B6 (full plane)
   virtual void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) = 0;
   virtual void refine_from(IEngine* coarse, int coarse_plane, int dst_plane) = 0;  // spectral zero-pad

@@ -556,27 +556,58 @@ class EngineT final : public IEngine {
   // scratch of the closure's batched transforms: 8 spectral planes, 8 mixed
   // planes, 8 real planes (allocated once, outside any stream capture)
   void closure_scratch() {
-    if (cl_w8_) return;
-    cl_w8_ = alloc<cpx<T>>(8 * S_);
+    if (cl_t8_) return;
     cl_t8_ = alloc<cpx<T>>(8 * S_);
     cl_r8_ = alloc<T>((size_t)8 * n_ * n_);
   }
   void closure_inputs(float* d_x, bool wait) override {
     // omega = -lap psi = k^2 psi, vz, d/dx and d/dy of psi, omega, vz: the 8
-    // spectral fields in one pass, one batched C2R (columns, then rows), one
-    // interleave into the FP32 NHWC tensor scaled by 1/n^2
+    // spectral fields formed as the column transforms load them, one batched
+    // row C2R, one interleave into the FP32 NHWC tensor scaled by 1/n^2
     if (wait) closure_scratch();
-    if (!cl_w8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
+    if (!cl_t8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
     const size_t cnt = (size_t)n_ * n_;
     const double s = 1.0 / ((double)n_ * n_);
-    k_closure_specs<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[P_PS], planes_[P_VZ], gd_, cl_w8_);
-    post("k_closure_specs");
-    launch_colfft<+1>(cl_w8_, cl_t8_, 8 * gd_.nh);
+    launch_closure_cols();
     launch_rowc2r(cl_t8_, cl_r8_, nullptr, 8);
     const Scale8 sc{{-s, s, s, s, -s, -s, s, s}};
     k_to_channels8<T><<<elem_blocks(cnt), 256, 0, st_>>>(cl_r8_, cnt, sc, d_x);
     post("k_to_channels8");
     if (wait) sync();
+  }
+  bool closure_fused() const override {
+    bool ok = false;
+    dispatch_n(n_, [&](auto NC) { ok = RowsCnn<T, decltype(NC)::value>::OK; });
+    return ok && nb_ == 1;
+  }
+  void closure_inputs_cnn(void* act0, const float* in_mean, const float* in_sd) override {
+    if (!cl_t8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
+    const double s = 1.0 / ((double)n_ * n_);
+    launch_closure_cols();
+    const Scale8 sc{{-s, s, s, s, -s, -s, s, s}};
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      if constexpr (RowsCnn<T, N>::OK) {
+        k_rows_to_cnn8<T, N><<<N / 2, RowsCnn<T, N>::THREADS, RowsCnn<T, N>::SMEM, st_>>>(
+            cl_t8_, sc, in_mean, in_sd, static_cast<__nv_bfloat16*>(act0), tw_);
+        post("k_rows_to_cnn8");
+      } else {
+        throw Error(kEINVAL, "fused closure path: n too large");
+      }
+    });
+  }
+  void set_closure_cnn(const float* y, const float* out_mean, const float* out_sd) override {
+    if (!cl_t8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      const int g = fft_groups((long long)(N / 2) * 2, C::G);
+      k_cnn2_to_rows<T, N><<<dim3((N / 2 + g - 1) / g, 2), C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(
+          y, out_mean, out_sd, cl_t8_, tw_);
+      post("k_cnn2_to_rows");
+    });
+    launch_colfft<-1>(cl_t8_, planes_[P_T5], 2 * gd_.nh, planes_[P_T6], gd_.nh);  // both tendency planes
+    closure_on_ = true;
   }
   void brackets() override { brackets_full(); }
   void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) override {
@@ -618,15 +649,14 @@ class EngineT final : public IEngine {
     }
     if (nb_ != 1) throw Error(kEINVAL, "the closure is a single-run feature");
     if (wait) closure_scratch();
-    if (!cl_w8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
+    if (!cl_t8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
     // the two channels as two real planes, one batched row R2C, the column
     // transforms into the tendency planes
     const size_t cnt = (size_t)n_ * n_;
     k_from_channels2<T><<<elem_blocks(cnt), 256, 0, st_>>>(d_t, cnt, cl_r8_);
     post("k_from_channels2");
     launch_rowr2c(cl_r8_, cl_t8_, 2);
-    launch_colfft<-1>(cl_t8_, planes_[P_T5], gd_.nh);
-    launch_colfft<-1>(cl_t8_ + S_, planes_[P_T6], gd_.nh);
+    launch_colfft<-1>(cl_t8_, planes_[P_T5], 2 * gd_.nh, planes_[P_T6], gd_.nh);  // both tendency planes
     // the tendency planes are fixed buffers: a captured step keyed on
     // closure_on_ stays valid across calls
     closure_on_ = true;
@@ -832,14 +862,27 @@ class EngineT final : public IEngine {
     while (g > 1 && (units + g - 1) / g < 2LL * sms_) g /= 2;
     return g;
   }
+  // the 8 closure-input fields of the state, y-transformed, into cl_t8_
+  void launch_closure_cols() {
+    dispatch_n(n_, [&](auto NC) {
+      constexpr int N = decltype(NC)::value;
+      using C = Cfg<T, N>;
+      const int ncols = 8 * gd_.nh;
+      const int g = fft_groups(ncols, C::G);
+      k_closure_cols<T, N><<<(ncols + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(
+          planes_[P_PS], planes_[P_VZ], gd_, cl_t8_, tw_);
+      post("k_closure_cols");
+    });
+  }
+  // (out2, split: columns from split on go to out2)
   template <int DIR>
-  void launch_colfft(const cpx<T>* in, cpx<T>* out, int ncols) {
+  void launch_colfft(const cpx<T>* in, cpx<T>* out, int ncols, cpx<T>* out2 = nullptr, int split = 0x7fffffff) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       using C = Cfg<T, N>;
       auto k = k_colfft<T, N, DIR>;
       const int g = fft_groups(ncols, C::G);
-      k<<<(ncols + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(in, out, ncols, tw_, 0);
+      k<<<(ncols + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(in, out, ncols, tw_, 0, out2, split);
       post("k_colfft");
     });
   }
@@ -852,7 +895,8 @@ class EngineT final : public IEngine {
       using C = Cfg<T, N>;
       auto k = k_colfft<T, N, -1, PY>;
       const int g = fft_groups(gd_.nh, C::G);
-      k<<<(gd_.nh + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(in, out, gd_.nh, tw_, gd_.nh);
+      k<<<(gd_.nh + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(in, out, gd_.nh, tw_, gd_.nh, nullptr,
+                                                                                   0x7fffffff);
       post("k_colfft");
     });
   }
@@ -967,6 +1011,9 @@ class EngineT final : public IEngine {
       set_smem_attr(k_colfft<T, N, -1, PassNT<T, N>::value>, sm);
       set_smem_attr(k_rowc2r<T, N>, sm);
       set_smem_attr(k_rowr2c<T, N>, sm);
+      set_smem_attr(k_cnn2_to_rows<T, N>, sm);
+      set_smem_attr(k_closure_cols<T, N>, sm);
+      if constexpr (RowsCnn<T, N>::OK) set_smem_attr(k_rows_to_cnn8<T, N>, RowsCnn<T, N>::SMEM);
       constexpr size_t smh = PassSmem<T, N>::SMEM;
       set_smem_attr(k_passA<T, N>, CfgA<T, N>::SMEM);
       set_smem_attr(k_passB<T, N, true>, smh);
@@ -1252,8 +1299,7 @@ class EngineT final : public IEngine {
   bool full_;
   int nb_ = 1, run_ = 0;
   bool closure_on_ = false;
-  cpx<T>* cl_w8_ = nullptr;  // closure scratch (closure_scratch)
-  cpx<T>* cl_t8_ = nullptr;
+  cpx<T>* cl_t8_ = nullptr;  // closure scratch (closure_scratch)
   T* cl_r8_ = nullptr;
   std::function<void(cudaStream_t)> hook_;
   unsigned long long hook_id_ = 0;

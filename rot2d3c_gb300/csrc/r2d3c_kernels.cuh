@@ -152,12 +152,13 @@ __device__ __forceinline__ T powi(T x, int k) {
 
 // --------------------------------------------------------------------------
 // generic y-direction transform of `ncols` contiguous columns of length N
-// (fftp2D.f90:208 forward, :251 inverse), in place allowed
+// (fftp2D.f90:208 forward, :251 inverse), in place allowed; columns from
+// `split` on go to out2 (two output planes of one launch)
 // --------------------------------------------------------------------------
 template <typename T, int N, int DIR, int PY = 1>
 __global__ void __launch_bounds__(Cfg<T, N>::THREADS)
 k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* __restrict__ tw,
-         int mx_in = 0) {
+         int mx_in = 0, cpx<T>* out2 = nullptr, int split = 0x7fffffff) {
   using C = Cfg<T, N>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
@@ -171,7 +172,7 @@ k_colfft(const cpx<T>* __restrict__ in, cpx<T>* out, int ncols, const tw_t<T>* _
     v[0][q] = ok ? in[mix_idx<N, PY>(col, lane + q * C::TPF, mx_in)] : czero<T>();
   F::template run<DIR>(v, lane, sm, tw);
   if (ok) {
-    cpx<T>* dst = out + (size_t)col * N;
+    cpx<T>* dst = col < split ? out + (size_t)col * N : out2 + (size_t)(col - split) * N;
 #pragma unroll
     for (int q = 0; q < C::E; ++q) dst[lane + q * C::TPF] = v[0][q];
   }
