@@ -557,9 +557,10 @@ int r2d3c_advance(r2d3c_ctx* ctx, int nsteps, int dt_mode, double cfl_or_dt, dou
   if (dt_mode == R2D3C_DT_FIXED) e->set_dt(cfl_or_dt);
   e->advance(ctx->mc(), nsteps, dt_mode == R2D3C_DT_CFL, cfl_or_dt, rf.empty() ? nullptr : rf.data());
   if (ctx->p.iflow == 2 && seed && seed1 && nsteps > 0) *seed = *seed1 = ctx->ci_final_seed;
-  if (time) *time = e->get_time();
-  if (dt_last) *dt_last = e->get_dt();
-  e->sync();
+  double dt = 0.0, t = 0.0;
+  e->get_dt_time(&dt, &t);  // one copy, one synchronisation
+  if (time) *time = t;
+  if (dt_last) *dt_last = dt;
   API_END
 }
 

@@ -315,6 +315,10 @@ static __global__ void k_cfl_dt(const unsigned long long* __restrict__ enc, cons
   if (add_time) scal[1] = __dadd_rn(scal[1], dt);
 }
 
+// one device scalar set from a kernel parameter (no host buffer to keep
+// alive, so no host synchronisation)
+static __global__ void k_set_scalar(double* p, double v) { *p = v; }
+
 static __global__ void k_add_time(double* scal, int nruns) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < nruns) scal[r * kScalStride + 1] = __dadd_rn(scal[r * kScalStride + 1], scal[r * kScalStride]);

@@ -85,6 +85,7 @@ class IEngine {
   virtual void set_time(double t) = 0;
   virtual double get_dt() = 0;
   virtual double get_time() = 0;
+  virtual void get_dt_time(double* dt, double* time) = 0;  // both with one copy
   virtual void mark_state_untruncated() = 0;
   // Batched engines hold nruns() runs of the same n that advance together;
   // per-run operations (state, forcing, diagnostics, dt, time) act on the run

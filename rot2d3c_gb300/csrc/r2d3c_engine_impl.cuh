@@ -358,6 +358,7 @@ class EngineT final : public IEngine {
     post("k_max_sq2");
     const CflCoef cc = cfl_coef(cfl, mc);
     cuda_check(cudaMemcpyAsync(d_cfl_ + run_, &cc, sizeof(cc), cudaMemcpyHostToDevice, st_), "H2D cfl coef");
+    coefs_valid_ = false;  // the device coefficients differ from the last upload_coefs
     k_cfl_dt<<<1, 1, 0, st_>>>(enc_, d_cfl_ + run_, scal_, 0, 1);
     post("k_cfl_dt");
     return get_dt();
@@ -368,6 +369,12 @@ class EngineT final : public IEngine {
   void set_time(double t) override { set_scal(1, t); }
   double get_dt() override { return get_scal(0); }
   double get_time() override { return get_scal(1); }
+  void get_dt_time(double* dt, double* time) override {
+    cuda_check(cudaMemcpyAsync(hsmall_, scal_, 2 * sizeof(double), cudaMemcpyDeviceToHost, st_), "D2H scal");
+    sync();
+    *dt = hsmall_[0];
+    *time = hsmall_[1];
+  }
   void mark_state_untruncated() override { dirty_[run_] = 1; }
   int nruns() const override { return nb_; }
   void select_run(int r) override {
@@ -665,6 +672,8 @@ class EngineT final : public IEngine {
 
  private:
   // per-run coefficient arrays: nb == 1 takes mc, a batch its run coefficients
+  // (skipped when the device already holds the same coefficients: a caller
+  // that advances one step per call pays no copy and no synchronisation)
   void upload_coefs(const ModelCoef& mc, double cfl) {
     if (nb_ == 1) coefs_.assign(1, mc);
     if ((int)coefs_.size() != nb_) throw Error(kESTATE, "run coefficients not set");
@@ -675,11 +684,16 @@ class EngineT final : public IEngine {
       sc[r] = StepCoef{m.nu, m.hnu, m.nuv, m.hnuv, 2 * m.omega, m.nn, m.mm, m.nnv, m.mmv};
       cc[r] = cfl_coef(cfl, m);
     }
-    cuda_check(cudaMemcpyAsync(d_sc_, sc.data(), sizeof(StepCoef) * nb_, cudaMemcpyHostToDevice, st_),
-               "H2D step coefs");
-    cuda_check(cudaMemcpyAsync(d_cfl_, cc.data(), sizeof(CflCoef) * nb_, cudaMemcpyHostToDevice, st_),
-               "H2D cfl coefs");
+    const size_t bs = sizeof(StepCoef) * nb_, bc = sizeof(CflCoef) * nb_;
+    if (coefs_valid_ && up_sc_.size() == bs && up_cc_.size() == bc && std::memcmp(up_sc_.data(), sc.data(), bs) == 0 &&
+        std::memcmp(up_cc_.data(), cc.data(), bc) == 0)
+      return;
+    cuda_check(cudaMemcpyAsync(d_sc_, sc.data(), bs, cudaMemcpyHostToDevice, st_), "H2D step coefs");
+    cuda_check(cudaMemcpyAsync(d_cfl_, cc.data(), bc, cudaMemcpyHostToDevice, st_), "H2D cfl coefs");
     sync();
+    up_sc_.assign(reinterpret_cast<const char*>(sc.data()), reinterpret_cast<const char*>(sc.data()) + bs);
+    up_cc_.assign(reinterpret_cast<const char*>(cc.data()), reinterpret_cast<const char*>(cc.data()) + bc);
+    coefs_valid_ = true;
   }
 
   template <typename U>
@@ -764,9 +778,8 @@ class EngineT final : public IEngine {
     return k < 0 ? 1.0 / r : r;
   }
   void set_scal(int i, double v) {
-    hsmall_[0] = v;
-    cuda_check(cudaMemcpyAsync(scal_ + i, hsmall_, sizeof(double), cudaMemcpyHostToDevice, st_), "H2D scal");
-    sync();
+    k_set_scalar<<<1, 1, 0, st_>>>(scal_ + i, v);
+    post("k_set_scalar");
   }
   double get_scal(int i) {
     cuda_check(cudaMemcpyAsync(hsmall_, scal_ + i, sizeof(double), cudaMemcpyDeviceToHost, st_), "D2H scal");
@@ -1155,6 +1168,7 @@ class EngineT final : public IEngine {
       {
         cuda_check(cudaMemsetAsync(pb_, 0, sizeof(cpx<T>) * 2 * S_ * nb_, st_), "memset");
         cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
+        coefs_valid_ = false;
         std::vector<std::pair<int, int>> cands;
         for (int g = GB; g >= 1; g /= 2) cands.push_back({0, g});
         if constexpr (kPipeC<T, N>) {
@@ -1325,6 +1339,8 @@ class EngineT final : public IEngine {
   CflCoef* d_cfl_ = nullptr;
   std::vector<char> dirty_;
   std::vector<ModelCoef> coefs_;
+  std::vector<char> up_sc_, up_cc_;  // the coefficients on the device (upload_coefs)
+  bool coefs_valid_ = false;
   cudaStream_t st_ = nullptr;
   bool ci_on_ = false;
   int ci_n_ = 0;
