@@ -57,7 +57,7 @@ enum { R2D3C_FIELD_PS = 0, R2D3C_FIELD_VZ = 1, R2D3C_FIELD_WW = 2, R2D3C_FIELD_I
 
 /* The 25 positional values of parameter.inp (read at Rot2D3C.para.f90:136-160)
    plus the grid size n (compile-time module grid in the reference,
-   pseudospec2D_mod.f90:101; a run-time value here). */
+   pseudospec2D_mod.f90:7-14; a run-time value here). */
 typedef struct r2d3c_params {
   int n;
   double cfl;      /*  1 (commented "dt" in parameter.inp, read as CFL) */
@@ -275,7 +275,7 @@ int r2d3c_poisson(r2d3c_ctx* ctx, const double* a, const double* b, double* c);
 int r2d3c_energy(r2d3c_ctx* ctx, const double* a, int kin, double* b);
 /* inerprod (:400-451) */
 int r2d3c_inerprod(r2d3c_ctx* ctx, const double* a, const double* b, int kin, double* rslt);
-/* randu (pseudospec2D_mod.f90:142-161): one draw, *seed updated */
+/* randu (pseudospec2D_mod.f90:52-71): one draw, *seed updated */
 float r2d3c_randu(int* seed);
 
 /* ---- allocation-free variant ------------------------------------------- */
@@ -286,7 +286,8 @@ float r2d3c_randu(int* seed);
    allowed); its scratch is a fixed file-scope device array, so n <= 512
    (larger n returns R2D3C_EINVAL), all calls on a device share that scratch
    (calls whose GPU work overlaps race), and the first call on each device
-   does the set-up (make it before any stream capture).  stream may be NULL. */
+   does the set-up, which ends with a device synchronisation (make it before
+   any stream capture).  stream may be NULL. */
 int r2d3c_fft_c2r_noalloc(int n, const double* d_in, double* d_out, void* stream);
 
 /* ---- measurement ------------------------------------------------------ */

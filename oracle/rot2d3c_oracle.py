@@ -33,12 +33,12 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-# var module, pseudospec2D_mod.f90:125
+# var module, pseudospec2D_mod.f90:34-39
 PI = 3.1415926535897932384
 
 
 # --------------------------------------------------------------------------
-# randu: pseudospec2D_mod.f90:142-161
+# randu: pseudospec2D_mod.f90:52-71
 # --------------------------------------------------------------------------
 _IQ, _IR, _MASK = 127773, 2836, 123459876
 _IA, _IM = 16807, 2147483647
@@ -51,7 +51,7 @@ def _i32(x: int) -> int:
 
 
 def randu(seed: list) -> float:
-    """XOR-masked Park-Miller step (Schrage), pseudospec2D_mod.f90:153-159.
+    """XOR-masked Park-Miller step (Schrage), pseudospec2D_mod.f90:63-69.
 
     ``seed`` is a one-element list standing for the Fortran INTEGER argument,
     which the routine updates in place.  The result is the REAL (float32)
@@ -260,7 +260,7 @@ def fluxes(fl0, fl1, fl2):
 @dataclass
 class Params:
     """The 25 positional values of parameter.inp (Rot2D3C.para.f90:136-160)
-    plus the grid size n (module grid, pseudospec2D_mod.f90:101)."""
+    plus the grid size n (module grid, pseudospec2D_mod.f90:7-14)."""
     n: int = 64
     cfl: float = 0.5
     step: int = 1

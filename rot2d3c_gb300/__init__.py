@@ -11,7 +11,7 @@ the reference's Fortran subroutines:
   ``energy``, ``inerprod``, ``CFL_condition``, ``cond_check``, ``spectrum``,
   ``transfers``, ``rand_force``, the RK step and the field outputs
   (src/pseudospec2D_Rot2D3C.f90, src/Rot2D3C.para.f90:393-615);
-* ``randu`` (src/pseudospec2D_mod.f90:142-161).
+* ``randu`` (src/pseudospec2D_mod.f90:52-71).
 
 Array layouts are the reference's Fortran layouts seen from C:
 spectral ``complex128[(n//2+1), n]`` indexed ``[kx][ky]`` and physical
@@ -55,7 +55,7 @@ def _phys_in(a, n):
 
 
 def randu(seed: list) -> float:
-    """randu (pseudospec2D_mod.f90:142-161) through the C-ABI; ``seed`` is a
+    """randu (pseudospec2D_mod.f90:52-71) through the C-ABI; ``seed`` is a
     one-element list updated in place like the Fortran INTEGER argument."""
     s = C.c_int(int(seed[0]))
     r = load().r2d3c_randu(C.byref(s))

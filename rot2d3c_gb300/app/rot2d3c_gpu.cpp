@@ -17,7 +17,7 @@
 // 4-byte markers) and time_field.txt (A3,F12.6).  Between outputs, whole
 // stretches of steps go to r2d3c_advance (CFL dt, forcing, RK step replayed
 // from one CUDA graph).  The grid size is a run-time value (fixed at compile
-// time in the reference, pseudospec2D_mod.f90:101).
+// time in the reference, pseudospec2D_mod.f90:7-14).
 #include <cerrno>
 #include <cinttypes>
 #include <cmath>

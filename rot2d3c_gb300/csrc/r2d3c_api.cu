@@ -47,9 +47,9 @@ std::string& last_error_slot() { return g_err; }
 
 namespace {
 
-constexpr double kPi = 3.1415926535897932384;  // module var (pseudospec2D_mod.f90:125)
+constexpr double kPi = 3.1415926535897932384;  // module var (pseudospec2D_mod.f90:34-39)
 
-// randu (pseudospec2D_mod.f90:142-161): XOR-masked Park-Miller step with
+// randu (pseudospec2D_mod.f90:52-71): XOR-masked Park-Miller step with
 // Schrage's factorisation in 32-bit integers; REAL (float) arithmetic for the
 // result.  *idum is updated in place like the Fortran INTEGER argument.
 float randu_impl(int* idum) {

@@ -14,7 +14,7 @@ because the diagnostics neither read dt nor touch the random seeds.
 
     python -m rot2d3c_gb300.driver --n 256 [--dir RUNDIR] [--fp32] [--max-steps K]
 
-The grid size is a run-time value here (module grid, pseudospec2D_mod.f90:101,
+The grid size is a run-time value here (module grid, pseudospec2D_mod.f90:7-14,
 fixes it at compile time in the reference).
 """
 from __future__ import annotations

@@ -20,7 +20,7 @@ from oracle import rot2d3c_oracle as O  # noqa: E402
 
 def main():
     out = {}
-    # randu stream from seed 1 (pseudospec2D_mod.f90:142-161)
+    # randu stream from seed 1 (pseudospec2D_mod.f90:52-71)
     s = [1]
     out["randu_seed1"] = np.array([O.randu(s) for _ in range(8)], dtype=np.float32)
     out["randu_seed1_final"] = np.array([s[0]])
