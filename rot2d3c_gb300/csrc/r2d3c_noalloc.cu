@@ -19,10 +19,13 @@
 //     transform reads is written by the column pass of the same call first,
 //     so nothing needs clearing;
 //   - the first call on each device performs the set-up (twiddle upload with
-//     cudaMemcpyToSymbol and cudaGetSymbolAddress of both arrays, with that
-//     device current); make that first call before any stream capture.
+//     cudaMemcpyToSymbol, a device synchronisation that makes the upload
+//     complete before any stream of the caller can read it, and
+//     cudaGetSymbolAddress of both arrays, with that device current); make
+//     that first call before any stream capture.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -50,7 +53,7 @@ static __device__ __align__(256) double2 g_noalloc_scratch[kScratchElems];
 static __device__ __align__(256) double2 g_noalloc_tw[kTwElems];
 
 struct DevSlot {
-  bool ready = false;
+  std::atomic<bool> ready{false};  // published (release) once the fields below are set
   double2* scratch = nullptr;  // device address of g_noalloc_scratch
   double2* tw = nullptr;       // device address of g_noalloc_tw
 };
@@ -82,13 +85,18 @@ void host_twiddles(int n, double2* out) {
 // current).  The host names of the arrays are only stand-ins; the kernels get
 // the device addresses returned by cudaGetSymbolAddress.
 DevSlot& setup(int dev) {
-  std::lock_guard<std::mutex> lk(g_mu);
   DevSlot& s = g_slots[dev];
-  if (s.ready) return s;
+  if (s.ready.load(std::memory_order_acquire)) return s;  // set-up done: no lock on the call path
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (s.ready.load(std::memory_order_relaxed)) return s;
   std::vector<double2> h(kTwElems);
   for (int n = 16; n <= kNoAllocMaxN; n <<= 1) host_twiddles(n, h.data() + tw_offset(n));
   cuda_check(cudaMemcpyToSymbol(g_noalloc_tw, h.data(), sizeof(double2) * kTwElems),
              "cudaMemcpyToSymbol(no-alloc twiddles)");
+  // A copy from pageable host memory may return before its DMA has landed,
+  // and the kernels run on the caller's stream, which need not wait for the
+  // legacy default stream (cudaStreamNonBlocking): finish the upload here.
+  cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize(no-alloc set-up)");
   void* p = nullptr;
   cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
   s.scratch = static_cast<double2*>(p);
@@ -96,7 +104,7 @@ DevSlot& setup(int dev) {
   cuda_check(cudaGetSymbolAddress(&p, g_noalloc_tw), "cudaGetSymbolAddress(no-alloc twiddles)");
   s.tw = static_cast<double2*>(p);
   // the column and row kernels of every n use dynamic shared memory below 48 KB
-  s.ready = true;
+  s.ready.store(true, std::memory_order_release);
   return s;
 }
 
