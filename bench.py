@@ -8,16 +8,25 @@ Omega = 10, a seeded random-phase initial spectrum ~ k^-3 for 1 <= |k| <= 100
 forcing in the shell 20 <= |k| <= 22 normalised like iflow = 1
 (energy(fp,1) = energy(fz,0) = 1).  All inputs are synthetic.
 
-One bench step = one RK4 step.  The headline `value` is the FP32 path
-(FP32 fields and transforms with compensated twiddles, FP64 reductions); the
-FP64 drop-in path is measured on the same workload and reported in `fp64`,
-with the relative L2 error of omega and vz of the FP32 path against FP64
-after 100 steps.
+One bench step = one RK4 step.  The headline `value` is the FP64 drop-in
+path (the reference's own arithmetic), device-timed over graph-replayed
+steps; `e2e` is the same path through the C-ABI with the state coming from
+and going back to pinned host FP64 buffers on every step; `e2e_loop` is the
+drop-in main loop (CFL time step every step, cond_check / spectrum +
+transfers / field output at a fixed cadence) through the C-ABI.  The FP32
+path (FP32 fields and transforms with compensated twiddles, FP64
+reductions) is reported in `fp32`, with its speed-up over FP64 and the
+relative L2 error of omega and vz against the FP64 path and against the
+CPU oracle after 100 steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-Multi-GPU: one field does not shard (replicas only); under torchrun every
-rank runs its own replica and `value` counts the steps of all ranks.
+Multi-GPU: one field does not shard (replicas only): every rank runs its own
+replica and `value` counts the steps of all ranks.  The batched ensemble
+leg partitions its runs over the ranks by cost (n^2 log2 n per step) and
+gathers the per-run diagnostics on the host.  `--gpus N` without a
+torchrun environment re-launches itself under torch.distributed.run with N
+ranks.
 """
 from __future__ import annotations
 
@@ -47,13 +56,19 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=WORKLOAD["n"])
-    ap.add_argument("--fp64-steps", type=int, default=0, help="timed FP64 steps (default: --steps)")
+    ap.add_argument("--fp32-steps", type=int, default=0, help="timed FP32 steps (default: --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="profiling runs of the FP32 path alone: skip the FP64 legs (the line then reports FP32)")
     ap.add_argument("--err-steps", type=int, default=100)
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-steps", type=int, default=500)
     ap.add_argument("--no-closure", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=20, help="steps of the host round-trip e2e leg")
+    ap.add_argument("--loop-steps", type=int, default=200, help="steps of the main-loop e2e leg (0: skip)")
+    ap.add_argument("--oracle-steps", type=int, default=100,
+                    help="CPU oracle steps for the error against the oracle and the CPU baseline (0: skip)")
     ap.add_argument("--closure-small", action="store_true",
                     help="closure leg on a small case (512^2 DNS, 128^2 LES, few steps): for profiling its kernels")
     return ap.parse_args()
@@ -129,6 +144,32 @@ def make_cparams(n):
     return R.make_params(n=n, nu=w["nu"], hnu=w["hnu"], nn=w["nn"], mm=w["mm"], nuv=w["nu"],
                          hnuv=w["hnu"], nnv=w["nn"], mmv=w["mm"], omega=w["omega"], iflow=0,
                          kup=w["f_kmax"], kdn=w["f_kmin"])
+
+
+def bench_config(n, world):
+    """The `config` of both arms (this one and `--impl reference`): the
+    same keys and values, so that the two lines describe one workload."""
+    return {"workload": f"single run {n}^2, RK4, dt=1e-4 fixed, nu=1e-5, hnu=0.1 (mm=2), Omega=10, "
+                        "IC k^-3 1<=|k|<=100, forcing shell 20-22",
+            "n": n, "precision": "FP64 (value: the reference's arithmetic); FP32 path reported in fp32",
+            "l2": "working set larger than L2 (state, forcing and six work planes: > 1 GB at 4096^2 FP64)",
+            "parallelism": f"replicas x{world}"}
+
+
+def maybe_spawn(args):
+    """--gpus N: under torchrun WORLD_SIZE must equal N; without it, N > 1
+    re-launches this script under torch.distributed.run with N ranks."""
+    ws = os.environ.get("WORLD_SIZE")
+    if ws is not None:
+        if int(ws) != args.gpus:
+            sys.stderr.write(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={ws}\n")
+            sys.exit(2)
+        return
+    if args.gpus > 1:
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", os.environ.get("MASTER_PORT", "29531"),
+               os.path.abspath(__file__)] + sys.argv[1:]
+        os.execv(sys.executable, cmd)
 
 
 # ---------------------------------------------------------------- clocks
@@ -208,15 +249,6 @@ def pass_bytes(n, real_bytes):
             "C": (2 * M * n + 6 * M * K + 2 * M * K) * c}
 
 
-def fft_flops_per_step(n):
-    """Nominal FFT FLOPs of one RK4 step of the fused path (5 L log2 L per
-    complex transform of length L): per substep 6 M column IFFTs (A), 4 n
-    packed row transforms (B), 2 M column FFTs (C)."""
-    M = n // 3 + 1
-    per = 5.0 * n * math.log2(n)
-    return 4 * (6 * M + 4 * n + 2 * M) * per
-
-
 def rel_err_fields(a_ps, a_vz, b_ps, b_vz, ka2):
     """Relative L2 errors of omega = k^2 psi and vz (half-plane weighted)."""
     import numpy as np
@@ -266,6 +298,146 @@ def replica_throughput(torch, world, steps_per_rank, elapsed_s, device="cuda"):
     return world * steps_per_rank / t, t
 
 
+
+
+def pass_flops(n):
+    """Nominal FFT FLOPs per launch of passes A, B, C (5 L log2 L per
+    complex transform of length L): A 6 M column IFFTs, B 4 n row
+    transforms (per row three packed inverse pairs and one packed forward
+    pair), C 2 M column FFTs."""
+    M = n // 3 + 1
+    per = 5.0 * n * math.log2(n)
+    return {"A": 6 * M * per, "B": 4 * n * per, "C": 2 * M * per}
+
+
+def pass_traffic(n, tag, top):
+    """DRAM bytes (read + write) per launch of pass `top` from the committed
+    ncu summary profiles/pass_traffic_<tag>_n<n>.json, or None."""
+    path = os.path.join(ROOT, "profiles", f"pass_traffic_{tag}_n{n}.json")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as f:
+        tr = json.load(f).get(f"k_pass{top}")
+    if not tr:
+        return None, None
+    return tr["dram_read"] + tr["dram_write"], os.path.relpath(path, ROOT) + " (ncu)"
+
+
+def roofline_of(ms, cnt, n, real_bytes, tag, hbm, peak_kind, peak64=None):
+    """HBM roofline of the top pass (algorithmic bytes per launch / CUDA-event
+    time per launch) with every pass's figures; for FP64 also the FP64-pipe
+    fraction (nominal FFT FLOPs / time against the measured FP64 FMA peak),
+    which is what binds that path."""
+    pb, pf = pass_bytes(n, real_bytes), pass_flops(n)
+    total = sum(ms[j] * cnt[j] for j in range(4))
+    passes = {}
+    for i, k in enumerate("ABC"):
+        d = {"ms_per_launch": ms[i], "algorithmic_bytes": pb[k],
+             "achieved_gbs": pb[k] / (ms[i] * 1e-3) / 1e9 if ms[i] > 0 else None,
+             "step_share": ms[i] * cnt[i] / total if total > 0 else None}
+        d["hbm_frac"] = d["achieved_gbs"] / hbm if d["achieved_gbs"] else None
+        if peak64:
+            d["fp64_tflops"] = pf[k] / (ms[i] * 1e-3) / 1e12 if ms[i] > 0 else None
+            d["fp64_pipe_frac"] = d["fp64_tflops"] / peak64 if d["fp64_tflops"] else None
+        passes[k] = d
+    top = max("ABC", key=lambda k: passes[k]["ms_per_launch"])
+    ach = passes[top]["achieved_gbs"]
+    traffic, tsrc = pass_traffic(n, tag, top)
+    r = {"bound": "hbm", "kernel": f"k_pass{top} ({'FP64' if real_bytes == 8 else 'FP32'}, n={n})",
+         "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_source": peak_kind,
+         "traffic": traffic, "traffic_source": tsrc, "algorithmic_bytes_per_launch": pb[top], "passes": passes}
+    if peak64:
+        r["fp64_pipe"] = {"achieved": passes[top]["fp64_tflops"], "peak": peak64, "unit": "TFLOP/s",
+                          "frac": passes[top]["fp64_pipe_frac"],
+                          "note": "what binds the FP64 path: nominal FFT FLOPs (5 L log2 L) per launch / "
+                                  "launch time, against the FP64 FMA throughput measured on this GPU "
+                                  "(r2d3c_fp64_fma_peak)"}
+    return r
+
+
+# ---------------------------------------------------------------- e2e legs
+def e2e_roundtrip(ctx, ps, vz, dt, steps, torch, world):
+    """The step through the C-ABI with the state owned by the host: every
+    step uploads psi-hat and vz-hat from pinned FP64 host buffers
+    (r2d3c_set_state), advances one RK4 step (r2d3c_advance) and reads the
+    new state back into pinned host buffers (r2d3c_get_state), the way a
+    caller that keeps its arrays in host memory would.  The two buffer pairs
+    alternate, so each step starts from the previous step's result.  Median
+    of three repetitions."""
+    import rot2d3c_gb300 as R
+    buf = [[torch.empty(a.shape, dtype=torch.complex128).pin_memory().numpy() for a in (ps, vz)]
+           for _ in range(2)]
+    els = []
+    for _ in range(3):
+        buf[0][0][...] = ps
+        buf[0][1][...] = vz
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for s in range(steps):
+            src, dst = buf[s % 2], buf[(s + 1) % 2]
+            ctx.set_state(src[0], src[1])                 # H2D of the state
+            ctx.advance(1, R.DT_FIXED, dt)                # one graph-replayed step (dt in, time out)
+            R.check(R.load().r2d3c_get_state(ctx._h, R._dptr(dst[0]), R._dptr(dst[1])), "get_state")  # D2H
+        els.append(time.perf_counter() - t0)
+    el = sorted(els)[1]
+    v, el = replica_throughput(torch, world, steps, el)
+    S = ps.size * 16
+    return {"value": v, "unit": UNIT, "h2d_bytes_per_step": 2 * S + 8, "d2h_bytes_per_step": 2 * S + 16,
+            "steps": steps, "repetitions": 3, "statistic": "median",
+            "path": "per step: r2d3c_set_state + r2d3c_advance(1) + r2d3c_get_state, pinned host FP64 buffers"}
+
+
+LOOP = dict(cstep=10, sstep=100, tstep=200, cfl=0.5)
+
+
+def e2e_main_loop(ctx, ps, vz, steps, torch, world):
+    """The drop-in main loop (Rot2D3C.para.f90:393-615) through the C-ABI:
+    the state comes from pinned host buffers once, then every step takes its
+    dt from the CFL condition (fused into the step), and at a fixed cadence
+    (the reference's parameter.inp cadence, cstep 100 / sstep 1000 / tstep
+    10000, divided by ten) the host receives cond_check's 30 values, the
+    energy spectra and the transfer functions, and the physical psi and vz
+    fields; the final state returns to the host."""
+    import rot2d3c_gb300 as R
+    L = LOOP
+    hin = [torch.empty(a.shape, dtype=torch.complex128).pin_memory().numpy() for a in (ps, vz)]
+    hout = [torch.empty(a.shape, dtype=torch.complex128).pin_memory().numpy() for a in (ps, vz)]
+    hin[0][...] = ps
+    hin[1][...] = vz
+    n = ctx.n
+    calls = {"cond_check": 0, "spectrum+transfers": 0, "fields": 0}
+    d2h = 0
+    ctx.set_time(0.0)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    ctx.set_state(hin[0], hin[1])
+    t = 0.0
+    for s in range(steps):
+        if s % L["cstep"] == 0:
+            ctx.cond_check(t)
+            calls["cond_check"] += 1
+            d2h += 30 * 8
+        if s % L["sstep"] == 0:
+            ctx.spectrum()
+            ctx.transfers()
+            calls["spectrum+transfers"] += 1
+            d2h += 5 * (n // 2 + 1) * 8
+        if s % L["tstep"] == 0:
+            ctx.get_field(R.FIELD_PS)
+            ctx.get_field(R.FIELD_VZ)
+            calls["fields"] += 1
+            d2h += 2 * n * n * 8
+        t, _ = ctx.advance(1, R.DT_CFL, L["cfl"])
+    R.check(R.load().r2d3c_get_state(ctx._h, R._dptr(hout[0]), R._dptr(hout[1])), "get_state")
+    el = time.perf_counter() - t0
+    v, el = replica_throughput(torch, world, steps, el)
+    S = ps.size * 16
+    return {"value": v, "unit": UNIT, "steps": steps, "seconds": el, "calls": calls,
+            "h2d_bytes_per_step": 2 * S / steps, "d2h_bytes_per_step": (d2h + 2 * S) / steps,
+            "cadence": dict(L, note="reference parameter.inp cadence (cstep 100, sstep 1000, tstep 10000) / 10; "
+                                    "dt from the CFL condition every step as in the reference")}
+
+
 # ---------------------------------------------------------------- ensemble
 ENSEMBLE = dict(groups=((512, 64), (1024, 16), (2048, 4)), omega_lo=0.1, omega_hi=100.0, hnu=0.1,
                 cfl=0.5, ic_kmin=1.0, ic_kmax=10.0, f_kmin=4.0, f_kmax=6.0, seed=7)
@@ -300,52 +472,74 @@ def ensemble_inputs():
     return runs
 
 
-def run_ensemble(args, torch):
-    """runs/s of the batched ensemble (all runs advance `steps` CFL steps in
-    one CUDA graph per step) and each run's total-energy budget residual
-    (BalanceTest_Rot2D3C.py: d/dt (E + Ez)/2 = inj - diss) over 100 steps."""
+def budget_residuals(S):
+    """Energy-budget residual of every run from cond_check samples S
+    [sample][run][30] (BalanceTest_Rot2D3C.py: d/dt (E + Ez)/2 = inj - diss):
+    |mean(dE/dt - (inj - diss))| / mean|inj| over the interior samples, dE/dt
+    by centred differences of the samples."""
     import numpy as np
-    import rot2d3c_gb300 as R
-    runs = ensemble_inputs()
-    groups = []
-    for n, count in ENSEMBLE["groups"]:
-        groups.append((n, [R.make_params(**r[1]) for r in runs if r[0] == n]))
-    ens = R.Ensemble(groups, R.FP32)
-    for i, (n, prm, ps, vz, fp, fz) in enumerate(runs):
-        ens.set_state(i, ps, vz)
-        ens.set_forcing(i, fp, fz)
-        ens.set_time(i, 0.0)
-    # budget: cond_check every 10 steps over 100 steps (outside the timed region)
-    samples = []
-    t = np.zeros(len(runs))
-    for k in range(11):
-        samples.append(np.array([ens.cond_check(i, t[i]) for i in range(len(runs))]))
-        if k < 10:
-            t = ens.advance(10, R.DT_CFL, ENSEMBLE["cfl"])
-    S = np.array(samples)  # [sample][run][30]
-    time = S[:, :, 0]
+    tm = S[:, :, 0]
     etot = 0.5 * (S[:, :, 1] + S[:, :, 2])
     inj = S[:, :, 3] + S[:, :, 4]
     diss = S[:, :, 5] + S[:, :, 6] + S[:, :, 7] + S[:, :, 8]
-    resid = []
-    for i in range(len(runs)):
-        dE = np.gradient(etot[:, i], time[:, i])
+    out = []
+    for i in range(S.shape[1]):
+        dE = np.gradient(etot[:, i], tm[:, i])
         r = dE - (inj[:, i] - diss[:, i])
-        resid.append(float(np.abs(np.mean(r[1:-1])) / max(np.mean(np.abs(inj[:, i])), 1e-300)))
-    resid = np.array(resid)
+        out.append(float(np.abs(np.mean(r[1:-1])) / max(np.mean(np.abs(inj[:, i])), 1e-300)))
+    return np.array(out)
+
+
+def run_ensemble(args, torch, rank=0, world=1):
+    """runs/s of the batched ensemble (every run advances `steps` CFL steps,
+    one CUDA graph per step holding every size group) and each run's
+    energy-budget residual.  With several ranks the runs are partitioned by
+    cost (rot2d3c_gb300.partition) and the per-run residuals are gathered
+    on the host; the time is the slowest rank's."""
+    import numpy as np
+    import rot2d3c_gb300 as R
+    from rot2d3c_gb300 import partition as P
+    runs = ensemble_inputs()
+    mine = P.partition([r[0] for r in runs], world)[rank]
+    groups = []
+    for n, _ in ENSEMBLE["groups"]:
+        ids = [i for i in mine if runs[i][0] == n]
+        if ids:
+            groups.append((n, [R.make_params(**runs[i][1]) for i in ids]))
+    order = [i for n, _ in ENSEMBLE["groups"] for i in mine if runs[i][0] == n]  # ensemble run -> global run
+    ens = R.Ensemble(groups, R.FP32)
+    for j, i in enumerate(order):
+        n, prm, ps, vz, fp, fz = runs[i]
+        ens.set_state(j, ps, vz)
+        ens.set_forcing(j, fp, fz)
+        ens.set_time(j, 0.0)
+    # budget: cond_check every 10 steps over 100 steps (outside the timed region)
+    samples = []
+    t = np.zeros(len(order))
+    for k in range(11):
+        samples.append(np.array([ens.cond_check(j, t[j]) for j in range(len(order))]))
+        if k < 10:
+            t = ens.advance(10, R.DT_CFL, ENSEMBLE["cfl"])
+    res_local = {i: float(r) for i, r in zip(order, budget_residuals(np.array(samples)))}
+    resid = np.array(P.gather_by_run(res_local, world, len(runs)))
     # timed: `steps` more steps of every run
     K = args.ensemble_steps
     ens.advance(3, R.DT_CFL, ENSEMBLE["cfl"])  # warm-up
     l0 = ens.kernel_launches()
+    dist_barrier(torch, world)
     torch.cuda.synchronize()
     t0 = time_mod.perf_counter()
     ens.advance(K, R.DT_CFL, ENSEMBLE["cfl"])
-    el = time_mod.perf_counter() - t0
+    el = dist_max(torch, world, time_mod.perf_counter() - t0)
+    worst = int(np.argmax(resid))
     out = {"value": len(runs) / el, "unit": f"runs/s ({K} RK4 steps per run)",
            "runs": len(runs), "groups": [list(g) for g in ENSEMBLE["groups"]], "steps_per_run": K,
            "seconds": el, "gpu_launches": ens.kernel_launches() - l0, "dtype": "f32 (FP64 reductions)",
+           "ranks": world, "partition": "runs dealt by cost n^2 log2 n (LPT), diagnostics gathered on the host",
            "plan": {str(g["n"]): plan_summary_dict(g["plan"]) for g in ens.plan_report()},
            "budget_residual": {"median": float(np.median(resid)), "max": float(resid.max()),
+                               "worst_run": {"index": worst, "n": runs[worst][0],
+                                             "omega": runs[worst][1]["omega"]},
                                "definition": "|mean(dE_tot/dt - (inj - diss))| / mean|inj| over 100 steps, "
                                              "cond_check every 10 steps"},
            "config": "64 x 512^2 + 16 x 1024^2 + 4 x 2048^2, Omega log-uniform [0.1,100], nu=1e-3(256/n)^2, "
@@ -383,31 +577,50 @@ def run_closure(small=False):
 
 
 # ---------------------------------------------------------------- CPU legs
-def cpu_baseline(n, ps, vz, fp, fz, budget_s=20.0):
-    """The C/OpenMP restatement of the reference step (oracle/cpu) on all host
-    cores: a bounded sample of the same workload."""
-    from oracle import cpu_oracle as CO
+CPU_FFT_NOTE = ("the C/OpenMP restatement's own radix-2 FFT (not FFTW, which the reference links: FFTW would "
+                "be faster by an unmeasured factor)")
+
+
+def oracle_params(n):
     from oracle import rot2d3c_oracle as O
     w = WORKLOAD
-    p = O.Params(n=n, nu=w["nu"], hnu=w["hnu"], nn=w["nn"], mm=w["mm"], nuv=w["nu"], hnuv=w["hnu"],
-                 nnv=w["nn"], mmv=w["mm"], omega=w["omega"], iflow=0)
+    return O.Params(n=n, nu=w["nu"], hnu=w["hnu"], nn=w["nn"], mm=w["mm"], nuv=w["nu"], hnuv=w["hnu"],
+                    nnv=w["nn"], mmv=w["mm"], omega=w["omega"], iflow=0)
+
+
+def cpu_leg(n, ps, vz, fp, fz, steps, budget_s=30.0):
+    """The C/OpenMP restatement of the reference step (oracle/cpu) from the
+    workload's initial state for `steps` steps on all host cores: the state
+    after `steps` steps (to check both GPU paths against) and, timed inside
+    that run, a bounded sample of its steps (the CPU baseline); plus one step
+    on one thread."""
+    from oracle import cpu_oracle as CO
+    p = oracle_params(n)
+    dt = WORKLOAD["dt"]
     th = CO.max_threads()
+    a, b, _ = CO.run(p, ps, vz, fp, fz, 1, dt, False, th)      # untimed first step
     t0 = time.perf_counter()
-    a, b, _ = CO.run(p, ps, vz, fp, fz, 1, w["dt"], False, th)
-    t1 = time.perf_counter()
-    per = t1 - t0
-    k = max(1, min(20, int(budget_s / max(per, 1e-6)) - 1))
+    a, b, _ = CO.run(p, a, b, fp, fz, 1, dt, False, th)
+    per = time.perf_counter() - t0
+    k = max(1, min(steps - 2, int(budget_s / max(per, 1e-6)) - 1)) if steps > 2 else 0
+    dtk = 0.0
+    if k:
+        t0 = time.perf_counter()
+        a, b, _ = CO.run(p, a, b, fp, fz, k, dt, False, th)
+        dtk = time.perf_counter() - t0
+    rest = steps - 2 - k
+    if rest > 0:
+        a, b, _ = CO.run(p, a, b, fp, fz, rest, dt, False, th)
     t0 = time.perf_counter()
-    CO.run(p, a, b, fp, fz, k, w["dt"], False, th)
-    dt = time.perf_counter() - t0
-    # one thread, one step (the reference's per-rank work without MPI)
-    t0 = time.perf_counter()
-    CO.run(p, a, b, fp, fz, 1, w["dt"], False, 1)
+    CO.run(p, a, b, fp, fz, 1, dt, False, 1)
     dt1 = time.perf_counter() - t0
-    return {"value": k / dt, "unit": UNIT, "cores": th, "kind": "port", "value_1thread": 1.0 / dt1,
-            "sample": f"{k} RK4 steps at {n}^2 FP64 (after 1 untimed), C/OpenMP restatement of the "
-                      f"reference step (35 C2R + 8 R2C per step as in the reference), {th} threads; "
-                      "value_1thread: 1 step on 1 thread; MPI ranks: 1 (threads instead of MPI)"}
+    v = (k + 1) / (dtk + per)
+    cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "value_1thread": 1.0 / dt1,
+           "sample": f"steps 2..{k + 2} of a {steps}-step run at {n}^2 FP64 from the workload's initial state, "
+                     f"{th} threads (MPI ranks: 1, threads instead of MPI); C/OpenMP restatement of the reference "
+                     f"step with the reference's cost structure (32 C2R + 8 R2C 2-D transforms per fixed-dt step), "
+                     f"FFT: {CPU_FFT_NOTE}; value_1thread: 1 step on 1 thread"}
+    return cpu, (a, b)
 
 
 def run_reference(args):
@@ -418,10 +631,8 @@ def run_reference(args):
     n = args.n
     ps, vz, fp, fz, _ = workload_inputs(n)
     from oracle import cpu_oracle as CO
-    from oracle import rot2d3c_oracle as O
+    p = oracle_params(n)
     w = WORKLOAD
-    p = O.Params(n=n, nu=w["nu"], hnu=w["hnu"], nn=w["nn"], mm=w["mm"], nuv=w["nu"], hnuv=w["hnu"],
-                 nnv=w["nn"], mmv=w["mm"], omega=w["omega"], iflow=0)
     th = CO.max_threads()
     warm = max(0, min(args.warmup, 5))  # the requested warm-up steps, at most 5 (about 3 s on 16 cores)
     a, b = ps, vz
@@ -438,13 +649,12 @@ def run_reference(args):
     el = time.perf_counter() - t0
     v = done / el
     sample = (f"{done} of {args.steps} requested RK4 steps at {n}^2 FP64 (bounded to ~60 s) after {warm} "
-              f"warm-up steps, "
-              f"C/OpenMP restatement of the reference step, {th} threads, MPI ranks: 1")
+              f"warm-up steps, C/OpenMP restatement of the reference step, {th} threads, MPI ranks: 1; "
+              f"FFT: {CPU_FFT_NOTE}")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
             "steps": done, "warmup": warm, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"single run {n}^2, RK4, dt=1e-4 fixed, nu=1e-5, hnu=0.1, Omega=10, "
-                                   "IC k^-3 1<=|k|<=100, forcing shell 20-22", "n": n},
+            "config": bench_config(n, world),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -453,6 +663,7 @@ def run_reference(args):
 # ---------------------------------------------------------------- main arm
 def main():
     args = parse()
+    maybe_spawn(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -461,7 +672,7 @@ def main():
         return
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
-    import numpy as np
+    import numpy as np  # noqa: F401
     import torch
     if world > 1:
         torch.cuda.set_device(0)
@@ -476,127 +687,97 @@ def main():
     K, W = args.steps, max(3, args.warmup)
     ps, vz, fp, fz, ka2 = workload_inputs(n)
     cp = make_cparams(n)
-
-    # ---- FP32 path: accuracy run, then timing
-    c32 = R.Context(cp, R.FP32)
-    c32.set_state(ps, vz)
-    c32.set_forcing(fp, fz)
-    out = {}
-    if not args.no_fp64:
-        c64 = R.Context(cp, R.FP64)
-        c64.set_state(ps, vz)
-        c64.set_forcing(fp, fz)
-        c64.advance(args.err_steps, R.DT_FIXED, dt)
-        c32.advance(args.err_steps, R.DT_FIXED, dt)
-        a64, b64 = c64.get_state()
-        a32, b32 = c32.get_state()
-        ew, ev = rel_err_fields(a32, b32, a64, b64, ka2)
-        out["err"] = {"rel_l2_omega": ew, "rel_l2_vz": ev, "after_steps": args.err_steps}
-        del a64, b64, a32, b32
-
-    c32.advance(W, R.DT_FIXED, dt)
-    dist_barrier(torch, world)
-    with ClockSampler(local if world == 1 else 0) as clk:
-        el32, launches32 = timed_advance(c32, K, dt, torch)
-        dist_barrier(torch, world)
-    v32, el32 = replica_throughput(torch, world, K, el32)
-    clocks = clk.summary()
-
-    # per-pass device times (CUDA events around each launch, separate pass)
-    ms32, cnt32 = c32.profile_passes(min(K, 20), dt)
     hbm, peak_kind = measured_peaks()
-    pb = pass_bytes(n, 4)
-    passes = {k: {"ms_per_launch": ms32[i], "algorithmic_bytes": pb[k],
-                  "achieved_gbs": pb[k] / (ms32[i] * 1e-3) / 1e9 if ms32[i] > 0 else None}
-              for i, k in enumerate("ABC")}
-    top = max("ABC", key=lambda k: passes[k]["ms_per_launch"])
-    ach = passes[top]["achieved_gbs"]
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"pass_traffic_fp32_n{n}.json")
-    if os.path.exists(tpath):  # DRAM bytes per launch from the committed ncu capture
-        with open(tpath) as f:
-            tr = json.load(f).get(f"k_pass{top}")
-        if tr:
-            traffic = tr["dram_read"] + tr["dram_write"]
-    roofline = {"bound": "hbm", "kernel": f"k_pass{top} (FP32, n={n})", "achieved": ach, "peak": hbm,
-                "unit": "GB/s", "frac": ach / hbm, "peak_source": peak_kind,
-                "traffic": traffic, "traffic_source": "profiles/pass_traffic_fp32_n4096.json (ncu)",
-                "algorithmic_bytes_per_launch": pass_bytes(n, 4)[top], "passes": passes,
-                "step_share": {k: ms32[i] * cnt32[i] / sum(ms32[j] * cnt32[j] for j in range(4))
-                               for i, k in enumerate("ABC")}}
 
-    # ---- e2e through the C-ABI with host buffers (FP32 path): the state goes
-    # in from and comes back to pinned host FP64 buffers (allocated before the
-    # timed region, as a caller that reuses its buffers would), and every step
-    # is one r2d3c_advance call (coefficients and dt in, time and dt out)
-    e2e_steps = min(K, 50)
-    hp_in = [torch.empty(a.shape, dtype=torch.complex128).pin_memory().numpy() for a in (ps, vz)]
-    hp_out = [torch.empty(a.shape, dtype=torch.complex128).pin_memory().numpy() for a in (ps, vz)]
-    hp_in[0][...] = ps
-    hp_in[1][...] = vz
-    # three repetitions, the median counts (host-side jitter of single runs)
-    els = []
-    for _ in range(3):
-        c32.synchronize()
-        t0 = time.perf_counter()
-        c32.set_state(hp_in[0], hp_in[1])           # H2D of the state
-        for _ in range(e2e_steps):
-            c32.advance(1, R.DT_FIXED, dt)          # H2D coefficients and dt, launch, D2H time and dt
-        R.check(R.load().r2d3c_get_state(c32._h, R._dptr(hp_out[0]), R._dptr(hp_out[1])), "get_state")  # D2H
-        els.append(time.perf_counter() - t0)
-    el_e2e = sorted(els)[1]
-    ve2e, el_e2e = replica_throughput(torch, world, e2e_steps, el_e2e)
-    S = (n // 2 + 1) * n * 16
-    e2e = {"value": ve2e, "unit": UNIT,
-           "h2d_bytes_per_step": (2 * S + 8 * e2e_steps) / e2e_steps,
-           "d2h_bytes_per_step": (2 * S + 16 * e2e_steps) / e2e_steps,
-           "steps": e2e_steps, "repetitions": 3, "statistic": "median",
-           "path": "r2d3c_set_state + per-step r2d3c_advance(1) + r2d3c_get_state (pinned host FP64 buffers)"}
+    def make(prec):
+        c = R.Context(cp, prec)
+        c.set_state(ps, vz)
+        c.set_forcing(fp, fz)
+        c.set_time(0.0)
+        return c
 
-    # ---- FP64 drop-in path
-    fp64 = None
-    if not args.no_fp64:
-        K64 = args.fp64_steps or K
+    # ---- accuracy runs (untimed): both paths from the same state, err_steps steps
+    c64 = None if args.no_fp64 else make(R.FP64)
+    c32 = None if (args.no_fp32 and not args.no_fp64) else make(R.FP32)
+    s64 = s32 = None
+    if c64 is not None:
+        c64.advance(args.err_steps, R.DT_FIXED, dt)
+        s64 = c64.get_state()
+    if c32 is not None:
+        c32.advance(args.err_steps, R.DT_FIXED, dt)
+        s32 = c32.get_state()
+
+    # ---- FP64 drop-in path: the headline
+    v64 = el64 = launches64 = roofline = e2e = e2e_loop = plan64 = clocks = None
+    if c64 is not None:
         c64.advance(W, R.DT_FIXED, dt)
-        el64, l64 = timed_advance(c64, K64, dt, torch)
-        v64, el64 = replica_throughput(torch, world, K64, el64)
-        ms64, cnt64 = c64.profile_passes(min(K64, 4), dt)
+        dist_barrier(torch, world)
+        with ClockSampler(local if world == 1 else 0) as clk:
+            el64, launches64 = timed_advance(c64, K, dt, torch)
+            dist_barrier(torch, world)
+        v64, el64 = replica_throughput(torch, world, K, el64)
+        clocks = clk.summary()
+        ms64, cnt64 = c64.profile_passes(min(K, 4), dt)
         peak64 = R.fp64_fma_peak()
-        flops = fft_flops_per_step(n)
-        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el64 / K64, "steps": K64,
-                "dtype": "f64", "fp32_speedup": v32 / v64,
-                "roofline": {"bound": "fp64", "achieved": flops * K64 / el64 / 1e12,
-                             "peak": peak64, "unit": "TFLOP/s",
-                             "frac": flops * K64 / el64 / 1e12 / peak64,
-                             "note": "nominal FFT FLOPs (5 L log2 L) per step / step time; peak "
-                                     "= measured FP64 FMA throughput on this GPU"},
-                "passes_ms_per_launch": dict(zip("ABC", ms64[:3]))}
-        fp64.update(out.get("err", {}))
+        roofline = roofline_of(ms64, cnt64, n, 8, "fp64", hbm, peak_kind, peak64)
+        e2e = e2e_roundtrip(c64, ps, vz, dt, min(K, args.e2e_steps), torch, world)
+        e2e_loop = e2e_main_loop(c64, ps, vz, args.loop_steps, torch, world) if args.loop_steps > 0 else None
+        plan64 = plan_summary(c64)
         c64.destroy()
 
-    ensemble = None if args.no_ensemble else run_ensemble(args, torch)
+    # ---- FP32 path
+    fp32 = None
+    if c32 is not None:
+        K32 = args.fp32_steps or K
+        c32.advance(W, R.DT_FIXED, dt)
+        dist_barrier(torch, world)
+        with ClockSampler(local if world == 1 else 0) as clk32:
+            el32, launches32 = timed_advance(c32, K32, dt, torch)
+            dist_barrier(torch, world)
+        v32, el32 = replica_throughput(torch, world, K32, el32)
+        ms32, cnt32 = c32.profile_passes(min(K32, 20), dt)
+        fp32 = {"value": v32, "unit": UNIT, "ms_per_step": 1e3 * el32 / K32, "steps": K32,
+                "dtype": "f32 (compensated twiddles, FP64 reductions)",
+                "fp32_speedup": v32 / v64 if v64 else None, "gpu_launches": launches32,
+                "roofline": roofline_of(ms32, cnt32, n, 4, "fp32", hbm, peak_kind),
+                "e2e": e2e_roundtrip(c32, ps, vz, dt, min(K32, 50), torch, world),
+                "clocks": clk32.summary(), "plan": plan_summary(c32)}
+        if s64 is not None:
+            ew, ev = rel_err_fields(s32[0], s32[1], s64[0], s64[1], ka2)
+            fp32["err_vs_fp64"] = {"rel_l2_omega": ew, "rel_l2_vz": ev, "after_steps": args.err_steps}
+        c32.destroy()
+    if c64 is None:  # FP32-only profiling run: the line reports the FP32 leg
+        v64, el64, K, launches64 = fp32["value"], fp32["ms_per_step"] * K32 / 1e3, K32, fp32["gpu_launches"]
+        roofline, e2e, clocks, plan64 = fp32["roofline"], fp32["e2e"], fp32["clocks"], fp32["plan"]
+
+    ensemble = None if args.no_ensemble else run_ensemble(args, torch, rank, world)
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(n, ps, vz, fp, fz)
+    err_oracle = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.oracle_steps > 0:
+        cpu, (oa, ob) = cpu_leg(n, ps, vz, fp, fz, args.oracle_steps)
+        if args.oracle_steps == args.err_steps:
+            err_oracle = {"after_steps": args.err_steps, "oracle": "C/OpenMP restatement (oracle/cpu), FP64"}
+            if s64 is not None:
+                ew, ev = rel_err_fields(s64[0], s64[1], oa, ob, ka2)
+                err_oracle["fp64"] = {"rel_l2_omega": ew, "rel_l2_vz": ev}
+            if s32 is not None:
+                ew, ev = rel_err_fields(s32[0], s32[1], oa, ob, ka2)
+                err_oracle["fp32"] = {"rel_l2_omega": ew, "rel_l2_vz": ev}
+                fp32["err_vs_oracle"] = err_oracle["fp32"]
     closure = None
     if rank == 0 and world == 1 and not args.no_closure:
         closure = run_closure(args.closure_small)
 
-    line = {"metric": METRIC, "value": v32, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": 1e3 * el32 / K, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (FP64 reductions)", "data": "synthetic",
-            "config": {"workload": f"single run {n}^2, RK4, dt=1e-4 fixed, nu=1e-5, hnu=0.1 (mm=2), "
-                                   "Omega=10, IC k^-3 1<=|k|<=100, forcing shell 20-22",
-                       "n": n, "precision": "FP32 path (headline) and FP64 path (fp64)",
-                       "l2": "working set larger than L2 (6 mixed planes of 268 MB at 4096^2 FP32)",
-                       "parallelism": f"replicas x{world}",
-                       "plan": plan_summary(c32)},
-            "gpu_launches": launches32, "roofline": roofline, "clocks": clocks, "e2e": e2e,
-            "fp64": fp64, "ensemble": ensemble, "closure": closure, "cpu_baseline": cpu}
+    line = {"metric": METRIC, "value": v64, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * el64 / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if not args.no_fp64 else "f32 (FP64 leg skipped)",
+            "data": "synthetic", "config": bench_config(n, world), "plan": plan64,
+            "gpu_launches": launches64, "roofline": roofline, "clocks": clocks, "e2e": e2e,
+            "e2e_loop": e2e_loop, "err_vs_oracle": err_oracle, "fp32": fp32, "ensemble": ensemble,
+            "closure": closure, "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    c32.destroy()
     if world > 1:
         torch.distributed.destroy_process_group()
 

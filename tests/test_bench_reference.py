@@ -9,11 +9,12 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _run(env_extra):
+def _run(env_extra, gpus=1, rc=0):
     env = dict(os.environ, **env_extra)
     r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n", "64", "--steps", "2",
-                        "--warmup", "3"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
-    assert r.returncode == 0, r.stderr[-2000:]
+                        "--warmup", "3", "--gpus", str(gpus)], cwd=ROOT, env=env, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == rc, r.stderr[-2000:]
     return [l for l in r.stdout.splitlines() if l.startswith("{")]
 
 
@@ -28,4 +29,18 @@ def test_reference_arm_line():
 
 
 def test_reference_arm_other_ranks_are_silent():
-    assert _run({"RANK": "1", "WORLD_SIZE": "2"}) == []
+    assert _run({"RANK": "1", "WORLD_SIZE": "2"}, gpus=2) == []
+
+
+def test_gpus_must_match_the_launched_world():
+    """--gpus N under a launcher whose WORLD_SIZE differs is an error, not a
+    silent single-GPU run."""
+    assert _run({"RANK": "0", "WORLD_SIZE": "1"}, gpus=2, rc=2) == []
+
+
+def test_both_arms_share_one_config():
+    sys.path.insert(0, ROOT)
+    import bench
+    lines = _run({})
+    d = json.loads(lines[0])
+    assert d["config"] == bench.bench_config(64, 1)
