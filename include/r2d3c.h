@@ -238,6 +238,15 @@ int r2d3c_cnn_set_normalization(r2d3c_cnn* cnn, const float* in_mean, const floa
 int r2d3c_closure_inputs(r2d3c_ctx* ctx, float* d_x);
 int r2d3c_closure_sample(r2d3c_ctx* fine, r2d3c_ctx* coarse, float* d_x, float* d_y);
 int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t);
+/* Per-shell weights of the tendencies: from now on the two tendencies are
+   multiplied, in spectral space, on shell b (kmn = int(sqrt(ka2)+.5),
+   b < nshells) by w[b] (omega tendency) and w[nshells + b] (vz tendency),
+   and by 0 beyond; nshells = 0 switches the weighting off (the default).
+   The closure experiment uses it to confine the network's tendencies to
+   the shells next to the cutoff, where the subgrid transfer acts.  Host
+   array of 2 nshells floats, copied before return (call it outside any
+   stream capture).  No counterpart in the reference. */
+int r2d3c_closure_set_band(r2d3c_ctx* ctx, const float* w, int nshells);
 /* nsteps LES steps with the network in the loop: before every RK step the
    8 inputs of the current state are formed, the network cnn (grid n x n) is
    evaluated on them and its two outputs are added to the brackets of that

@@ -86,6 +86,73 @@ def set_tendency(ctx, d_t) -> None:
     check(load().r2d3c_closure_set_tendency(ctx._h, None if d_t is None else _ptr(d_t)), "closure_set_tendency")
 
 
+def set_band(ctx, w) -> None:
+    """Per-shell weights of ctx's learned tendencies (r2d3c_closure_set_band):
+    ``w`` is [2, nshells] (omega tendency, vz tendency) or None (off)."""
+    if w is None:
+        check(load().r2d3c_closure_set_band(ctx._h, None, 0), "closure_set_band")
+        return
+    w = np.ascontiguousarray(w, np.float32)
+    assert w.ndim == 2 and w.shape[0] == 2
+    check(load().r2d3c_closure_set_band(ctx._h, C.c_void_p(w.ctypes.data), w.shape[1]), "closure_set_band")
+
+
+def shell_index(n: int) -> np.ndarray:
+    """Shell kmn = int(sqrt(ka2) + .5) of every element of an [kx][ky]
+    spectral plane of an n^2 grid (the engine's shell rule)."""
+    h = n // 2
+    ka = np.concatenate([np.arange(h), np.arange(h) - h]).astype(np.float64)
+    k2 = ka[: h + 1, None] ** 2 + ka[None, :] ** 2
+    return np.floor(np.sqrt(k2) + 0.5).astype(np.int64)
+
+
+def band_fit(net: CNN, X, Y, idx, n: int, batch: int = 8):
+    """Per-shell skill of the network on the snapshots ``idx`` (held-out
+    data): for each tendency c and shell b the least-squares weight
+    w = sum Re(P conj T) / sum |P|^2 over the shell's modes, clipped to
+    [0, 1], where P and T are the spectra of the prediction and of the
+    target; shells where the prediction is uncorrelated with the target get
+    weights near 0.  The spectra come from the library's own FP64 transform
+    on the device.  Returns [2, n/2+1] float32."""
+    import torch
+    from . import FP64, R2C, FFTPlan
+    batch = max(1, min(batch, net.max_batch))
+    nb = n // 2 + 1
+    sh = shell_index(n)
+    two = np.full(sh.shape, 2.0)
+    two[0] = 1.0
+    keep = sh < nb  # the corners beyond shell n/2 lie outside every retained mode
+    sh, two = sh[keep], two[keep]
+    num = np.zeros((2, nb))
+    den = np.zeros((2, nb))
+    plan = FFTPlan(n, R2C, FP64)
+    out = torch.empty((batch, n, n, 2), dtype=torch.float32, device="cuda")
+    phys = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    spec = torch.empty((nb, n, 2), dtype=torch.float64, device="cuda")
+
+    def r2c(field):
+        phys.copy_(field)
+        plan.r2c_dev(phys.data_ptr(), spec.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        s = spec.cpu().numpy()
+        return (s[..., 0] + 1j * s[..., 1])[keep]
+    idx = list(idx)
+    for i0 in range(0, len(idx), batch):
+        ids = idx[i0:i0 + batch]
+        xb = X[ids].contiguous()
+        net.forward(xb, len(ids), out)
+        torch.cuda.synchronize()
+        for j, i in enumerate(ids):
+            for c in range(2):
+                P = r2c(out[j, :, :, c])
+                T = r2c(Y[i, :, :, c])
+                num[c] += np.bincount(sh, two * (P * np.conj(T)).real, minlength=nb)
+                den[c] += np.bincount(sh, two * np.abs(P) ** 2, minlength=nb)
+    plan.destroy()
+    with np.errstate(divide="ignore", invalid="ignore"):
+        w = np.where(den > 0, num / den, 0.0)
+    return np.clip(w, 0.0, 1.0).astype(np.float32)
+
+
 def closure_advance(ctx, net: CNN, nsteps: int, dt_mode: int, cfl_or_dt: float):
     """nsteps LES steps of ctx with the network evaluated before every step
     (one captured CUDA graph per step).  Returns (time, dt of the last step)."""

@@ -1122,6 +1122,15 @@ int r2d3c_closure_set_tendency(r2d3c_ctx* ctx, const float* d_t) {
   API_END
 }
 
+int r2d3c_closure_set_band(r2d3c_ctx* ctx, const float* w, int nshells) {
+  API_BEGIN
+  REQUIRE(ctx, "NULL argument");
+  REQUIRE(nshells >= 0 && nshells <= ctx->p.n / 2 + 1, "nshells must be in [0, n/2+1]");
+  REQUIRE(nshells == 0 || w, "NULL weights");
+  ctx->eng->set_closure_band(w, nshells);
+  API_END
+}
+
 int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
                           double* time, double* dt_last) {
   API_BEGIN

@@ -121,6 +121,12 @@ class IEngine {
   virtual void refine_from(IEngine* coarse, int coarse_plane, int dst_plane) = 0;  // spectral zero-pad
   virtual void closure_targets(IEngine* fine, float* d_y) = 0;
   virtual void set_closure(const float* d_t, bool wait) = 0;
+  // Per-shell weights (shell b = int(sqrt(ka2)+.5), b < nw; beyond nw: 0)
+  // applied to the tendency planes by every later set_closure /
+  // set_closure_cnn: w[b] to the first, w[nw + b] to the second; nw = 0
+  // switches the weighting off.  Host array of 2 nw floats, copied
+  // (synchronously: call outside any capture).
+  virtual void set_closure_band(const float* w, int nw) = 0;
   // Work queued on the engine stream before every step of advance(), inside
   // the captured graph (id != 0; id identifies the hook for the graph cache,
   // and id 0 removes it).

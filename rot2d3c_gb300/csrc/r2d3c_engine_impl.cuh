@@ -449,7 +449,7 @@ class EngineT final : public IEngine {
       sync();  // seq goes out of scope
     }
     upload_coefs(mc, cfl);
-    GraphKey key{cfl_mode, rf != nullptr, closure_on_, hook_ ? hook_id_ : 0ull};
+    GraphKey key{cfl_mode, rf != nullptr, closure_on_, band_nw_ > 0, hook_ ? hook_id_ : 0ull};
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
@@ -547,10 +547,10 @@ class EngineT final : public IEngine {
   // The captured step depends only on these; coefficients and dt live in
   // device arrays read by the kernels, so changing them needs no recapture.
   struct GraphKey {
-    bool cfl_mode = false, rf = false, closure = false;
+    bool cfl_mode = false, rf = false, closure = false, band = false;
     unsigned long long hook = 0;
     bool same(const GraphKey& o) const {
-      return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure && hook == o.hook;
+      return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure && band == o.band && hook == o.hook;
     }
   };
   static bool batched(int p) { return p <= P_C2; }  // ps, vz, fp, fz, c1, c2
@@ -614,7 +614,18 @@ class EngineT final : public IEngine {
       post("k_cnn2_to_rows");
     });
     launch_colfft<-1>(cl_t8_, planes_[P_T5], 2 * gd_.nh, planes_[P_T6], gd_.nh);  // both tendency planes
+    band_weight();
     closure_on_ = true;
+  }
+  void set_closure_band(const float* w, int nw) override {
+    if (nw < 0 || nw > gd_.nh) throw Error(kEINVAL, "closure band: 0 <= nshells <= n/2+1");
+    if (nw > 0 && !w) throw Error(kEINVAL, "closure band: NULL weights");
+    if (nw > 0) {
+      if (!band_w_) band_w_ = alloc<float>(2 * (size_t)gd_.nh);
+      cuda_check(cudaMemcpyAsync(band_w_, w, sizeof(float) * 2 * nw, cudaMemcpyHostToDevice, st_), "band upload");
+      sync();
+    }
+    band_nw_ = nw;
   }
   void brackets() override { brackets_full(); }
   void coarsen_from(IEngine* fine, int fine_plane, int dst_plane) override {
@@ -664,6 +675,7 @@ class EngineT final : public IEngine {
     post("k_from_channels2");
     launch_rowr2c(cl_r8_, cl_t8_, 2);
     launch_colfft<-1>(cl_t8_, planes_[P_T5], 2 * gd_.nh, planes_[P_T6], gd_.nh);  // both tendency planes
+    band_weight();
     // the tendency planes are fixed buffers: a captured step keyed on
     // closure_on_ stays valid across calls
     closure_on_ = true;
@@ -671,6 +683,12 @@ class EngineT final : public IEngine {
   }
 
  private:
+  // the per-shell weights of set_closure_band on both tendency planes
+  void band_weight() {
+    if (band_nw_ <= 0) return;
+    k_shell_weight2<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[P_T5], planes_[P_T6], gd_, band_w_, band_nw_);
+    post("k_shell_weight2");
+  }
   // per-run coefficient arrays: nb == 1 takes mc, a batch its run coefficients
   // (skipped when the device already holds the same coefficients: a caller
   // that advances one step per call pays no copy and no synchronisation)
@@ -1314,6 +1332,8 @@ class EngineT final : public IEngine {
   int nb_ = 1, run_ = 0;
   bool closure_on_ = false;
   cpx<T>* cl_t8_ = nullptr;  // closure scratch (closure_scratch)
+  float* band_w_ = nullptr;  // per-shell tendency weights (set_closure_band)
+  int band_nw_ = 0;
   T* cl_r8_ = nullptr;
   std::function<void(cudaStream_t)> hook_;
   unsigned long long hook_id_ = 0;

@@ -62,6 +62,39 @@ def test_step_with_subgrid_tendencies(gpu, prec, tol):
     set_tendency(c, None)
 
 
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 1e-5)])
+def test_band_weights_scale_each_shell_of_the_tendencies(gpu, prec, tol):
+    """r2d3c_closure_set_band: the tendencies enter the step multiplied per
+    shell by the omega / vz weights (0 beyond the weighted shells)."""
+    import torch
+    from rot2d3c_gb300.closure import set_band, set_tendency, shell_index
+    n = 32
+    p, cp = params(n, omega=1.0, nu=1e-3, hnu=0.1, nuv=1e-3, hnuv=0.1, iflow=0)
+    g, ps, vz = random_state(n, 18, amp=10.0)
+    fp, fz = random_forcing(g, 19)
+    rng = np.random.default_rng(3)
+    t = np.stack([O.c2r(g, O.random_phase_field(g, 1, 12, -1.0, rng)) for _ in range(2)], axis=-1)
+    t = (t / n**2 * 1e3).astype(np.float32)
+    nw = 10  # shells 10 and beyond get weight 0
+    w = rng.uniform(0.0, 1.0, (2, nw)).astype(np.float32)
+    c = gpu.Context(cp, prec)
+    c.set_state(ps, vz)
+    c.set_forcing(fp, fz)
+    set_band(c, w)
+    set_tendency(c, torch.from_numpy(t).cuda())
+    c.advance(2, gpu.DT_FIXED, 1e-3)
+    sh = shell_index(n)
+    fac = [np.where(sh < nw, w[k][np.minimum(sh, nw - 1)].astype(np.float64), 0.0) for k in range(2)]
+    tau5 = fac[0] * O.r2c(g, t[..., 0].astype(np.float64))
+    tau6 = fac[1] * O.r2c(g, t[..., 1].astype(np.float64))
+    for _ in range(2):
+        ps, vz, fp, fz = O.rk_step(g, p, ps, vz, fp, fz, 1e-3, tau5=tau5, tau6=tau6)
+    a, b = c.get_state()
+    assert rel_l2(a, ps) < tol and rel_l2(b, vz) < tol, (rel_l2(a, ps), rel_l2(b, vz))
+    set_tendency(c, None)
+    set_band(c, None)
+
+
 def test_cnn_normalisation_maps_units(gpu):
     import torch
     from oracle import cnn_oracle as CO
@@ -80,13 +113,14 @@ def test_cnn_normalisation_maps_units(gpu):
     assert np.linalg.norm(out.cpu().numpy() - ref) <= 1e-2 * np.linalg.norm(ref)
 
 
-@pytest.mark.parametrize("prec", [0, 1])
-def test_graph_captured_les_steps_equal_the_step_by_step_loop(gpu, prec):
+@pytest.mark.parametrize("prec,band", [(0, False), (1, False), (1, True)])
+def test_graph_captured_les_steps_equal_the_step_by_step_loop(gpu, prec, band):
     """r2d3c_closure_advance (inputs, network, tendencies and the RK step in
     one captured graph) gives bit-identical states to the same steps made one
-    call at a time, in both dt modes; the tendencies are off afterwards."""
+    call at a time, in both dt modes, with and without per-shell weights;
+    the tendencies are off afterwards."""
     import torch
-    from rot2d3c_gb300.closure import CNN, closure_advance, closure_inputs, set_tendency
+    from rot2d3c_gb300.closure import CNN, closure_advance, closure_inputs, set_band, set_tendency
     n = 32
     _, cp = params(n, omega=1.0, nu=2e-3, nuv=2e-3, hnu=0.1, hnuv=0.1, iflow=0)
     g, ps, vz = random_state(n, 41, amp=20.0)
@@ -100,6 +134,8 @@ def test_graph_captured_les_steps_equal_the_step_by_step_loop(gpu, prec):
             c.set_state(ps, vz)
             c.set_forcing(fp, fz)
             c.set_time(0.0)
+            if band:
+                set_band(c, np.linspace(1.0, 0.2, 2 * 12, dtype=np.float32).reshape(2, 12))
         x = torch.empty((1, n, n, 8), dtype=torch.float32, device="cuda")
         t = torch.empty((1, n, n, 2), dtype=torch.float32, device="cuda")
         for _ in range(5):

@@ -25,6 +25,33 @@ def test_les_workflow_small(gpu):
         assert all(math.isfinite(v) for v in e.values()), (name, e)
 
 
+# A small case of the closure experiment: 512^2 DNS (nu = 1e-4, Omega = 1,
+# hypoviscosity 1 with mm = 2, forcing shell 4-6), 400 snapshots filtered to
+# 128^2 (k_c = 42), 2000 Adam steps, four 3000-step coarse runs per model
+# from held-out snapshots.
+GAIN_CASE = dict(nf=512, nc=128, omega=1.0, nu=1e-4, hnu=1.0, nsnap=400, snap_every=10, spinup=3000,
+                 train_steps=2000, batch=32, lr=5e-4, les_steps=3000, cfl=0.5, seed=1, starts=4)
+
+
+@pytest.mark.gpu
+def test_trained_closure_beats_the_plain_and_hyperviscous_coarse_runs(gpu):
+    """What the trained network gains: the LES (network tendencies on the
+    shells next to the cutoff) is closer to the filtered DNS than both the
+    plain coarse solver and the hyperviscous fallback on every energy-spectrum
+    measure up to k_c (energy-weighted, shape, top third of the shells, worst
+    shell), and its energy flux is better than the plain run's and within 5%
+    of the fallback's."""
+    from rot2d3c_gb300.les import run_experiment
+
+    r = run_experiment(**GAIN_CASE)
+    e = r["spectrum_error"]
+    print({k: {m: round(v, 3) for m, v in d.items()} for k, d in e.items()})
+    for m in ("rel_l1", "mean_abs_log10", "rel_l1_top_third", "max_shell_rel"):
+        assert e["les"][m] < e["plain"][m] and e["les"][m] < e["fallback"][m], (m, e)
+    assert e["les"]["flux_rel_l1"] < e["plain"]["flux_rel_l1"]
+    assert e["les"]["flux_rel_l1"] < 1.05 * e["fallback"]["flux_rel_l1"]
+
+
 def test_coarse_forcing_is_the_same_physical_field():
     """The coarse copy of the forcing, transformed to physical space, equals
     the fine forcing sampled on every (nf/nc)-th grid point (all its modes are
