@@ -220,6 +220,14 @@ int r2d3c_cnn_forward(r2d3c_cnn* cnn, const float* d_x, int batch, float* d_out)
    receives dloss/dparams */
 int r2d3c_cnn_gradients(r2d3c_cnn* cnn, const float* d_x, const float* d_y, int batch, float* host_grad,
                         double* loss);
+/* Vector-Jacobian product at the inputs d_x: given d_gout = dL/d(output)
+   ([batch][H][W][2], physical output units), d_gx (may be NULL) receives
+   dL/dx ([batch][H][W][8]) and host_grad (may be NULL) dL/dparams.  The
+   forward pass is recomputed inside, so the call needs nothing kept from an
+   earlier forward; operands are BF16 as in training.  Synchronous on
+   return.  For autograd bindings (rot2d3c_gb300/torch_ops.py). */
+int r2d3c_cnn_backward(r2d3c_cnn* cnn, const float* d_x, const float* d_gout, int batch, float* d_gx,
+                       float* host_grad);
 /* forward, backward and one Adam step (beta 0.9/0.999, eps 1e-8) */
 int r2d3c_cnn_train_step(r2d3c_cnn* cnn, const float* d_x, const float* d_y, int batch, float lr, double* loss);
 /* per-channel standardisation applied inside the network: inputs are mapped

@@ -97,3 +97,32 @@ def loss_and_grads(params, x, t, emulate=True):
         g = r(da * gelu_d(pres[l - 1]))
     flat = np.concatenate([np.concatenate([dw.ravel(), db]) for dw, db in grads])
     return loss, flat
+
+
+def vjp(params, x, g_out, emulate=True):
+    """Vector-Jacobian product of the network at the (standardised) input x
+    for dL/d(output) = g_out: returns (dL/dparams flat, dL/dx), rounding to
+    bfloat16 where the GPU kernels round (the output gradient, every
+    back-propagated activation gradient)."""
+    r = bf16 if emulate else (lambda v: np.asarray(v, np.float64))
+    layers = split(params)
+    out, acts, pres = forward(params, x, emulate)
+    g = r(g_out)
+    grads = [None] * len(layers)
+    dx = None
+    for l in range(len(layers) - 1, -1, -1):
+        w, b = layers[l]
+        a = acts[l]
+        dw = np.zeros_like(w)
+        for tap in range(9):
+            dy, dx_ = divmod(tap, 3)
+            xs = np.roll(a, shift=(-(dy - 1), -(dx_ - 1)), axis=(1, 2))
+            dw[tap] = np.einsum("bijc,bijo->co", xs, g)
+        grads[l] = (dw, g.sum(axis=(0, 1, 2)))
+        da = r(conv_t(g, r(w)))
+        if l == 0:
+            dx = da
+            break
+        g = r(da * gelu_d(pres[l - 1]))
+    flat = np.concatenate([np.concatenate([dw.ravel(), db]) for dw, db in grads])
+    return flat, dx

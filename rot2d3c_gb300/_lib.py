@@ -110,6 +110,7 @@ SIGNATURES = {
     "r2d3c_cnn_forward": (C.c_int, [_P, _P, C.c_int, _P]),
     "r2d3c_cnn_gradients": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(C.c_float), _D]),
     "r2d3c_cnn_train_step": (C.c_int, [_P, _P, _P, C.c_int, C.c_float, _D]),
+    "r2d3c_cnn_backward": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(C.c_float)]),
     "r2d3c_cnn_set_normalization": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                               C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "r2d3c_closure_inputs": (C.c_int, [_P, _P]),

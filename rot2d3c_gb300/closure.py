@@ -16,6 +16,17 @@ def _ptr(t) -> C.c_void_p:
     return C.c_void_p(t if isinstance(t, int) else t.data_ptr())
 
 
+def _ready(*ts) -> None:
+    """The library's kernels run on their own non-blocking streams, which do
+    not wait for torch's: before a call reads or writes torch tensors, the
+    work torch has queued on them must be complete."""
+    for t in ts:
+        if t is not None and not isinstance(t, int):
+            import torch
+            torch.cuda.current_stream(t.device).synchronize()
+            return
+
+
 class CNN:
     """The closure network on an H x W periodic grid (see include/r2d3c.h)."""
 
@@ -44,17 +55,29 @@ class CNN:
         check(load().r2d3c_cnn_set_normalization(self._h, *ptrs), "cnn_set_normalization")
 
     def forward(self, x, batch: int, out) -> None:
+        _ready(x, out)
         check(load().r2d3c_cnn_forward(self._h, _ptr(x), batch, _ptr(out)), "cnn_forward")
 
     def gradients(self, x, y, batch: int):
         g = np.empty(self.nparams, np.float32)
         loss = C.c_double()
+        _ready(x, y)
         check(load().r2d3c_cnn_gradients(self._h, _ptr(x), _ptr(y), batch, g.ctypes.data_as(C.POINTER(C.c_float)),
                                          C.byref(loss)), "cnn_gradients")
         return loss.value, g
 
+    def backward(self, x, gout, batch: int, gx=None):
+        """Vector-Jacobian product at x (r2d3c_cnn_backward): dL/dx into gx
+        (optional) for dL/d(output) = gout; returns dL/dparams."""
+        g = np.empty(self.nparams, np.float32)
+        _ready(x, gout, gx)
+        check(load().r2d3c_cnn_backward(self._h, _ptr(x), _ptr(gout), batch, None if gx is None else _ptr(gx),
+                                        g.ctypes.data_as(C.POINTER(C.c_float))), "cnn_backward")
+        return g
+
     def train_step(self, x, y, batch: int, lr: float = 1e-3) -> float:
         loss = C.c_double()
+        _ready(x, y)
         check(load().r2d3c_cnn_train_step(self._h, _ptr(x), _ptr(y), batch, lr, C.byref(loss)), "cnn_train_step")
         return loss.value
 
@@ -72,17 +95,20 @@ class CNN:
 
 def closure_inputs(ctx, d_x) -> None:
     """The 8 network inputs of ctx's current state into d_x ([n, n, 8] FP32)."""
+    _ready(d_x)
     check(load().r2d3c_closure_inputs(ctx._h, _ptr(d_x)), "closure_inputs")
 
 
 def closure_sample(fine, coarse, d_x, d_y) -> None:
     """Filter fine's state onto coarse; inputs and subgrid targets of it."""
+    _ready(d_x, d_y)
     check(load().r2d3c_closure_sample(fine._h, coarse._h, _ptr(d_x), _ptr(d_y)), "closure_sample")
 
 
 def set_tendency(ctx, d_t) -> None:
     """Subgrid tendencies ([n, n, 2] FP32, physical) added to the brackets of
     the following steps of ctx; None switches them off."""
+    _ready(d_t)
     check(load().r2d3c_closure_set_tendency(ctx._h, None if d_t is None else _ptr(d_t)), "closure_set_tendency")
 
 

@@ -600,6 +600,29 @@ __global__ void k_mse(const float* __restrict__ out, const float* __restrict__ t
   if (threadIdx.x == 0) lpart[blockIdx.x] = red[0];
 }
 
+// dY of the last layer from a caller's output gradient g = dL/d(out) in
+// physical output units: out = y * std + mean, so dL/dy = g * std (bf16,
+// padded to 16 channels, zero beyond 2)
+__global__ void k_gout(const float* __restrict__ g, size_t npix, const float* __restrict__ tsd,
+                       bf16* __restrict__ dy) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix * 16; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t p = i >> 4;
+    const int c = (int)(i & 15);
+    dy[i] = __float2bfloat16_rn(c < 2 ? g[p * 2 + c] * tsd[c] : 0.f);
+  }
+}
+
+// dL/dx (FP32 NHWC, 8 channels) from the gradient of the network's
+// standardised bf16 input (16 channels): x' = (x - mean) / std
+__global__ void k_gin(const bf16* __restrict__ da, size_t npix, const float* __restrict__ sd,
+                      float* __restrict__ gx) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix * 8; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t p = i >> 3;
+    const int c = (int)(i & 7);
+    gx[i] = __bfloat162float(da[p * 16 + c]) / sd[c];
+  }
+}
+
 // Adam on FP32 master weights; also writes the bf16 forward weights
 // wf[k][co] (padded shapes) and the backward-data weights wb[k'][ci] with
 // k' = (8 - tap)*COUTP + co.
@@ -831,6 +854,20 @@ struct r2d3c_cnn {
     const float scale = 1.0f / (float)(npix * 2);
     k_mse<<<256, 256, 0, st>>>(pre[kLayers - 1], tgt, npix, scale, norm + 16, norm + 18, dY, lpart);
     cuda_check(cudaGetLastError(), "k_mse");
+    backprop(B, nullptr);
+    std::vector<float> lp(256);
+    cuda_check(cudaMemcpyAsync(lp.data(), lpart, 256 * sizeof(float), cudaMemcpyDeviceToHost, st), "D2H loss");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    double s = 0.0;
+    for (float v : lp) s += v;
+    return s / (double)(npix * 2);
+  }
+
+  // From dY = dL/dy of the last layer (as the forward pass left it, with
+  // the hidden pre-activations kept): the parameter gradients into grad[]
+  // and, when gx is set, dL/dx of the FP32 input into gx
+  void backprop(int B, float* gx) {
+    const size_t npix = (size_t)B * H * W;
     for (int l = kLayers - 1; l >= 0; --l) {
       const Layer& ly = L[l];
       // dY holds dL/dy of layer l (bf16, coutp channels)
@@ -841,18 +878,20 @@ struct r2d3c_cnn {
       cuda_check(cudaGetLastError(), "k_reduce_parts");
       // unpad into grad (layout [9][cin][cout], then the bias)
       unpad_wgrad(l, part + (size_t)nparts * kc);
-      if (l == 0) break;
-      // dA of layer l-1 = conv(dY, wb[l]); then dY' = dA * gelu'(pre[l-1])
+      // dA of layer l's input = conv(dY, wb[l]) (backward data)
+      if (l == 0) {
+        if (gx) {
+          conv(0, dY, wb[0], B, nullptr, dA, 0, false, true);
+          k_gin<<<1024, 256, 0, st>>>(dA, npix, norm + 8, gx);
+          cuda_check(cudaGetLastError(), "k_gin");
+        }
+        break;
+      }
+      // then dY' = dA * gelu'(pre[l-1])
       conv(l, dY, wb[l], B, nullptr, dA, 0, false, true);
       k_gelu_back<<<1024, 256, 0, st>>>(dA, pre[l - 1], npix * L[l - 1].coutp, dY);
       cuda_check(cudaGetLastError(), "k_gelu_back");
     }
-    std::vector<float> lp(256);
-    cuda_check(cudaMemcpyAsync(lp.data(), lpart, 256 * sizeof(float), cudaMemcpyDeviceToHost, st), "D2H loss");
-    cuda_check(cudaStreamSynchronize(st), "sync");
-    double s = 0.0;
-    for (float v : lp) s += v;
-    return s / (double)(npix * 2);
   }
 
   void unpad_wgrad(int l, const float* gp) {
@@ -1103,6 +1142,28 @@ int r2d3c_cnn_gradients(r2d3c_cnn* c, const float* d_x, const float* d_y, int ba
     const double l = c->backward(d_y, batch);
     c->check_err();
     if (loss) *loss = l;
+    if (host_grad) {
+      cuda_check(cudaMemcpyAsync(host_grad, c->grad, c->nparam * sizeof(float), cudaMemcpyDeviceToHost, c->st),
+                 "D2H");
+      cuda_check(cudaStreamSynchronize(c->st), "sync");
+    }
+  } catch (const Error& e) {
+    return fail(e);
+  }
+  return R2D3C_OK;
+}
+
+int r2d3c_cnn_backward(r2d3c_cnn* c, const float* d_x, const float* d_gout, int batch, float* d_gx,
+                       float* host_grad) {
+  try {
+    if (!c || !d_x || !d_gout) throw Error(kEINVAL, "NULL argument");
+    if (batch < 1 || batch > c->Bmax) throw Error(kEINVAL, "batch out of range");
+    c->forward(d_x, batch, true);
+    const size_t npix = (size_t)batch * c->H * c->W;
+    k_gout<<<1024, 256, 0, c->st>>>(d_gout, npix, c->norm + 18, c->dY);
+    cuda_check(cudaGetLastError(), "k_gout");
+    c->backprop(batch, d_gx);
+    c->check_err();
     if (host_grad) {
       cuda_check(cudaMemcpyAsync(host_grad, c->grad, c->nparam * sizeof(float), cudaMemcpyDeviceToHost, c->st),
                  "D2H");
