@@ -7,6 +7,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -957,13 +959,25 @@ class EngineT final : public IEngine {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       constexpr int NT = PassNT<T, N>::value;
-      using C = CfgA<T, N>;
-      auto k = k_passA<T, N>;
-      const int groups = (gd_.M + NT - 1) / NT;
-      const int g = ga_ ? ga_ : C::G;  // groups per CTA, field chunks: autotuned
-      const dim3 grid((groups + g - 1) / g, nb, fa_);
-      k<<<grid, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(a, b, tf, gd_, tw_a_, batch());
-      post("k_passA");
+      auto go = [&](auto EC) {
+        constexpr int EA = decltype(EC)::value;
+        using C = CfgAE<T, N, EA>;
+        auto k = k_passA<T, N, EA>;
+        const int groups = (gd_.M + NT - 1) / NT;
+        const int g = ga_ ? ga_ : C::G;  // groups per CTA, field chunks: autotuned
+        const dim3 grid((groups + g - 1) / g, nb, fa_);
+        // each radix has the twiddle table of its own stage schedule
+        const tw_t<T>* tw = EA == PassAE<T, N>::value ? tw_a_ : tw_;
+        k<<<grid, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(a, b, tf, gd_, tw, batch());
+        post("k_passA");
+      };
+      if constexpr (kAltRadixA<T, N>) {
+        if (radix_a_ == Cfg<T, N>::E) {
+          go(std::integral_constant<int, Cfg<T, N>::E>{});
+          return;
+        }
+      }
+      go(std::integral_constant<int, PassAE<T, N>::value>{});
     });
   }
   template <bool CFL>
@@ -1047,6 +1061,7 @@ class EngineT final : public IEngine {
       if constexpr (RowsCnn<T, N>::OK) set_smem_attr(k_rows_to_cnn8<T, N>, RowsCnn<T, N>::SMEM);
       constexpr size_t smh = PassSmem<T, N>::SMEM;
       set_smem_attr(k_passA<T, N>, CfgA<T, N>::SMEM);
+      if constexpr (kAltRadixA<T, N>) set_smem_attr(k_passA<T, N, Cfg<T, N>::E>, CfgAE<T, N, Cfg<T, N>::E>::SMEM);
       set_smem_attr(k_passB<T, N, true>, smh);
       set_smem_attr(k_passB<T, N, false>, smh);
       set_smem_attr(k_passC<T, N>, smh);
@@ -1097,8 +1112,11 @@ class EngineT final : public IEngine {
   //      or half of that;
   //   C: the same with column pairs.
   // Small grids gain from spreading the work over more SMs (256^2: the
-  // config's groups fill 6 CTAs in pass A); large ones from full CTAs.  The
-  // transform radices, which change the rounding, are fixed per n.
+  // config's groups fill 6 CTAs in pass A); large ones from full CTAs.
+  // Pass A's radix (FP32, n = 1024 .. 4096) is chosen as FFTW's measured
+  // plans choose their algorithms: it changes the rounding (both radices
+  // stay within the FP32 path's error bound against FP64), so the choice is
+  // made once per process for each precision and n (choose_plan).
   // Time per launch (us) of each of nc candidates: one untimed launch of
   // every candidate, then three rounds over all of them (interleaved, so that
   // clock or cache drift affects them alike), each round three launches of a
@@ -1148,19 +1166,29 @@ class EngineT final : public IEngine {
       const int saved = launches_;
       int sms = 0;
       cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
-      // ---- pass A (reads the state, writes the derivative planes)
+      // ---- pass A (reads the state, writes the derivative planes): every
+      // radix it has (FP32 n = 1024 .. 4096: 16 and 8) x groups per CTA x
+      // field chunks
       cuda_check(cudaMemsetAsync(tf_, 0, sizeof(cpx<T>) * 6 * (size_t)gd_.M * n_ * nb_, st_), "memset");
       {
-        std::vector<std::pair<int, int>> cands;  // (groups per CTA, field chunks)
-        for (int g = GA; g >= 1; g /= 2)
-          for (int f : {1, 2, 3, 6}) cands.push_back({g, f});
+        struct CandA {
+          int radix, g, f;
+        };
+        std::vector<CandA> cands;
+        std::vector<std::pair<int, int>> radices = {{PassAE<T, N>::value, GA}};
+        if constexpr (kAltRadixA<T, N>) radices.push_back({Cfg<T, N>::E, CfgAE<T, N, Cfg<T, N>::E>::G});
+        for (auto [r, G] : radices)
+          for (int g = G; g >= 1; g /= 2)
+            for (int f : {1, 2, 3, 6}) cands.push_back({r, g, f});
         const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
-          ga_ = cands[i].first;
-          fa_ = cands[i].second;
+          radix_a_ = cands[i].radix;
+          ga_ = cands[i].g;
+          fa_ = cands[i].f;
           launch_passA(pbase_[P_PS], pbase_[P_VZ], tf_, nb_);
         });
         tune_a_.clear();
-        for (size_t i = 0; i < cands.size(); ++i) tune_a_.push_back({cands[i].first, cands[i].second, us[i]});
+        for (size_t i = 0; i < cands.size(); ++i)
+          tune_a_.push_back({cands[i].g, cands[i].f, us[i], cands[i].radix});
       }
       // (mode, grid): mode 0 one CTA per row / column pair with `grid` groups
       // per CTA; mode 1 persistent with `grid` CTAs
@@ -1233,8 +1261,41 @@ class EngineT final : public IEngine {
         return k;
       };
       const int pol = policy_;
-      const size_t ka = argmin(tune_a_, [&](const TuneRec& r) { return pol == 0 || (r.mode == GA && r.grid == 1); });
-      ga_ = forced[0] >= 0 ? (forced[0] ? forced[0] : GA) : tune_a_[ka].mode;
+      // pass A's radix: R2D3C_RADIX_A, else the choice already made in this
+      // process for this precision and n, else the default radix unless the
+      // other one's best candidate is more than 3% faster (then remembered
+      // for the process, so that every engine of this precision and n --
+      // single runs and batched ones alike -- rounds the same way)
+      const int r0 = PassAE<T, N>::value;
+      int ra = r0;
+      if constexpr (kAltRadixA<T, N>) {
+        const int r1 = Cfg<T, N>::E;
+        if (const char* e = std::getenv("R2D3C_RADIX_A")) {
+          ra = std::atoi(e);
+          if (ra != r0 && ra != r1)
+            throw Error(kEINVAL, "R2D3C_RADIX_A must be " + std::to_string(r0) + " or " + std::to_string(r1));
+        } else {
+          std::lock_guard<std::mutex> lk(radix_mu());
+          auto& cache = radix_cache();
+          const int key = (int)sizeof(T) * 1000000 + N;
+          auto it = cache.find(key);
+          if (it != cache.end()) {
+            ra = it->second;
+          } else {
+            const size_t b0 = argmin(tune_a_, [&](const TuneRec& r) { return r.radix == r0; });
+            const size_t b1 = argmin(tune_a_, [&](const TuneRec& r) { return r.radix == r1; });
+            if (b1 < tune_a_.size() && tune_a_[b1].us < 0.97f * tune_a_[b0].us) ra = r1;
+            cache[key] = ra;
+          }
+        }
+      }
+      radix_a_ = ra;
+      const int GAr = ra == r0 ? GA : CfgAE<T, N, Cfg<T, N>::E>::G;
+      const size_t ka = argmin(tune_a_, [&](const TuneRec& r) {
+        return r.radix == ra && (pol == 0 || (r.mode == GAr && r.grid == 1));
+      });
+      if (forced[0] > GAr) throw Error(kEINVAL, "R2D3C_GROUPS: more pass-A groups per CTA than its radix allows");
+      ga_ = forced[0] >= 0 ? (forced[0] ? forced[0] : GAr) : tune_a_[ka].mode;
       fa_ = forced[1] >= 0 ? forced[1] : tune_a_[ka].grid;
       auto pick_bc = [&](const std::vector<TuneRec>& t, const char* env, const char* pair_name, int forced_g,
                          int& mode, int& grid, int& groups) {
@@ -1275,11 +1336,12 @@ class EngineT final : public IEngine {
     std::string r = "{\"policy\": " + std::to_string(policy_) + ", \"pass_a\": [";
     char b[200];
     for (size_t i = 0; i < tune_a_.size(); ++i) {
-      snprintf(b, sizeof b, "%s{\"groups\": %d, \"field_chunks\": %d, \"us\": %.2f}", i ? ", " : "",
-               tune_a_[i].mode, tune_a_[i].grid, (double)tune_a_[i].us);
+      snprintf(b, sizeof b, "%s{\"radix\": %d, \"groups\": %d, \"field_chunks\": %d, \"us\": %.2f}",
+               i ? ", " : "", tune_a_[i].radix, tune_a_[i].mode, tune_a_[i].grid, (double)tune_a_[i].us);
       r += b;
     }
-    snprintf(b, sizeof b, "], \"groups_a\": %d, \"field_chunks_a\": %d, \"pass_b\": [", ga_, fa_);
+    snprintf(b, sizeof b, "], \"radix_a\": %d, \"groups_a\": %d, \"field_chunks_a\": %d, \"pass_b\": [",
+             radix_a_, ga_, fa_);
     r += b;
     for (size_t i = 0; i < tune_.size(); ++i) {
       if (tune_[i].mode)
@@ -1350,7 +1412,18 @@ class EngineT final : public IEngine {
   struct TuneRec {
     int mode, grid;  // pass A: groups, field chunks; B, C: variant, CTAs or groups
     float us;
+    int radix = 0;  // pass A: the transform radix
   };
+  // pass A radix chosen per (precision, n), shared by the engines of a process
+  static std::map<int, int>& radix_cache() {
+    static std::map<int, int> m;
+    return m;
+  }
+  static std::mutex& radix_mu() {
+    static std::mutex m;
+    return m;
+  }
+  int radix_a_ = 0;  // pass A radix (0 before the plan: the default)
   std::vector<TuneRec> tune_a_, tune_, tune_c_;
   cpx<T>* pbase_[P_COUNT] = {};
   double* scal_base_ = nullptr;

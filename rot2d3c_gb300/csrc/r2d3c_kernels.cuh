@@ -81,6 +81,12 @@ template <typename T, int N> struct PassAE {
 // registers the interleaved float4 exchange measured slower)
 template <typename T, int N>
 using CfgA = Cfg<T, N, PassNT<T, N>::value, PassAE<T, N>::value, PassAE<T, N>::value != 16>;
+// Pass A with radix EA (the plan autotuner may pick the other radix where
+// two exist: FP32, n = 1024 .. 4096, radix 16 or 8)
+template <typename T, int N, int EA>
+using CfgAE = Cfg<T, N, PassNT<T, N>::value, EA, EA != 16>;
+template <typename T, int N>
+constexpr bool kAltRadixA = PassAE<T, N>::value != Cfg<T, N>::E;
 
 // Shared memory of passes B and C: NT transform buffers per group, plus (when
 // it fits) a store for the first transform's result, which is held across the
@@ -291,15 +297,15 @@ k_rowr2c(const T* __restrict__ rin, cpx<T>* __restrict__ tout, const tw_t<T>* __
 // tiled mode each group transforms two adjacent columns at once and writes
 // both as 16-byte column pairs of the pair-tiled plane.
 // --------------------------------------------------------------------------
-template <typename T, int N>
-__global__ void __launch_bounds__(CfgA<T, N>::THREADS, (sizeof(T) == 4 && CfgA<T, N>::THREADS == 256) ? 2 : 1)
+template <typename T, int N, int EA = PassAE<T, N>::value>
+__global__ void __launch_bounds__(CfgAE<T, N, EA>::THREADS, (sizeof(T) == 4 && CfgAE<T, N, EA>::THREADS == 256) ? 2 : 1)
 k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __restrict__ tf,
         DevGrid gd, const tw_t<T>* __restrict__ tw, Batch bs) {
   constexpr int NT = PassNT<T, N>::value;
   ps += blockIdx.y * bs.spec;
   vz += blockIdx.y * bs.spec;
   tf += blockIdx.y * bs.tf;
-  using C = CfgA<T, N>;
+  using C = CfgAE<T, N, EA>;
   using F = typename C::FFT;
   R2D3C_SMEM_DECL
   const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;

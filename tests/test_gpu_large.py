@@ -148,3 +148,29 @@ def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
     monkeypatch.setenv("R2D3C_GROUPS", "3,1,1,1")
     with pytest.raises(gpu.R2D3CError):
         gpu.Context(cp, prec)
+
+
+@pytest.mark.parametrize("n", [1024, 4096])
+def test_fp32_pass_a_radices_stay_within_the_fp32_bound(gpu, monkeypatch, n):
+    """The plan autotuner may run FP32 pass A with radix 16 or 8 (they round
+    differently, like FFTW's measured plans): each radix, forced, steps
+    within the FP32 path's bound of the FP64 path, and every engine of one
+    precision and n in a process uses the same radix."""
+    cp, ps, vz, fp, fz = _case(n, 13)
+    a64, b64, _, _ = _advance(gpu, 0, cp, ps, vz, fp, fz, 3, gpu.DT_CFL, 0.5)
+    for radix in (16, 8):
+        monkeypatch.setenv("R2D3C_RADIX_A", str(radix))
+        c = gpu.Context(cp, 1)
+        rep = c.plan_report()
+        assert rep["radix_a"] == radix and {r["radix"] for r in rep["pass_a"]} == {8, 16}
+        c.set_state(ps, vz)
+        c.set_forcing(fp, fz)
+        c.set_time(0.0)
+        c.advance(3, gpu.DT_CFL, 0.5)
+        a, b = c.get_state()
+        c.destroy()
+        assert rel_l2(a, a64) < 1e-5 and rel_l2(b, b64) < 1e-5, (radix, rel_l2(a, a64), rel_l2(b, b64))
+    monkeypatch.delenv("R2D3C_RADIX_A")
+    r1 = gpu.Context(cp, 1).plan_report()["radix_a"]
+    r2 = gpu.Context(cp, 1).plan_report()["radix_a"]
+    assert r1 == r2 and r1 in (8, 16)
