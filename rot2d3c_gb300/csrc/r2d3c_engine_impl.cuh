@@ -1006,8 +1006,9 @@ class EngineT final : public IEngine {
         auto k = k_passB<T, N, CFL>;
         const int g = gb_ ? gb_ : C::G;  // groups per CTA: autotuned
         const dim3 grid((N / NR + g - 1) / g, nb);
-        k<<<grid, C::TPF * g, g * PassSmem<T, N>::GROUP_ELEMS * sizeof(cpx<T>), st_>>>(tf, pb, kxo, gd_, inv4, tw_,
-                                                                                      enc_base_, batch());
+        // (the rolled form keeps each group's first bracket in shared memory too)
+        const size_t smem = g * (PassSmem<T, N>::GROUP_ELEMS * sizeof(cpx<T>) + (RolledB<T, N>::OK ? N * sizeof(T) : 0));
+        k<<<grid, C::TPF * g, smem, st_>>>(tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
         post("k_passB");
       }
     });
@@ -1062,8 +1063,8 @@ class EngineT final : public IEngine {
       constexpr size_t smh = PassSmem<T, N>::SMEM;
       set_smem_attr(k_passA<T, N>, CfgA<T, N>::SMEM);
       if constexpr (kAltRadixA<T, N>) set_smem_attr(k_passA<T, N, Cfg<T, N>::E>, CfgAE<T, N, Cfg<T, N>::E>::SMEM);
-      set_smem_attr(k_passB<T, N, true>, smh);
-      set_smem_attr(k_passB<T, N, false>, smh);
+      set_smem_attr(k_passB<T, N, true>, RolledB<T, N>::SMEM);
+      set_smem_attr(k_passB<T, N, false>, RolledB<T, N>::SMEM);
       set_smem_attr(k_passC<T, N>, smh);
       if constexpr (kPipeC<T, N>) {
         set_smem_attr(k_passC_pipe<N>, PipeC<N>::SMEM);

@@ -450,6 +450,18 @@ __device__ __forceinline__ void cfl_max_sq(const cpx<T> (&v)[NT][E], unsigned lo
   if ((threadIdx.x & 31) == 0) atomicMax(enc, enc_ordered((double)m));
 }
 
+// Pass B with one rolled copy of the transform code (a loop over the four
+// transforms that is not unrolled) and the first bracket p1 in shared
+// memory, for the FP32 grid with one row per group (n = 8192): unrolled,
+// the compiler interleaves the four 8192-point transforms and spills
+// hundreds of bytes per thread.  The forward transform is the inverse one
+// of the conjugate, conjugated: bit-identical to the unrolled form.
+template <typename T, int N>
+struct RolledB {
+  static constexpr bool OK = sizeof(T) == 4 && PassNT<T, N>::value == 1 && PassSmem<T, N>::HOLD;
+  static constexpr size_t SMEM = PassSmem<T, N>::SMEM + (OK ? (size_t)Cfg<T, N, 1>::G * N * sizeof(T) : 0);
+};
+
 template <typename T, int N, bool CFL>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
@@ -473,6 +485,46 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
   const int M = gd.M;
   const size_t plane = (size_t)M * N;
   cpx<T> v[NR][C::E];
+  if constexpr (RolledB<T, N>::OK) {
+    T* P1 = reinterpret_cast<T*>(smbase_ + (size_t)(blockDim.x / C::TPF) * PS::GROUP_ELEMS) + (size_t)g * N;
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+      if (f < 3) {
+        const cpx<T>* pa = tf + (size_t)(2 * f) * plane;
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          cpx<T> z[1];
+          packed_pair<T, N, 1>(pa, pa + plane, lane + q * C::TPF, y0, M, z);
+          v[0][q] = z[0];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) v[0][q].y = -v[0][q].y;
+      }
+      F::template run<+1>(v, lane, sm, tw);
+      // each thread reads back only the positions it wrote: no barrier needed
+      if (f == 0) {
+        if constexpr (CFL) cfl_max_sq<T, 1, C::E>(v, cfl_enc);
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) hold[lane + q * C::TPF] = v[0][q];
+      } else if (f == 1) {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          const cpx<T> a = hold[lane + q * C::TPF];
+          P1[lane + q * C::TPF] = (a.x * v[0][q].y - a.y * v[0][q].x) * inv_n4;
+        }
+      } else if (f == 2) {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          const cpx<T> a = hold[lane + q * C::TPF];
+          v[0][q] = mkc<T>(P1[lane + q * C::TPF], (a.x * v[0][q].y - a.y * v[0][q].x) * inv_n4);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) v[0][q].y = -v[0][q].y;
+      }
+    }
+  } else {
   cpx<T> z1r[HOLD ? 1 : NR][C::E];
   T p1[NR][C::E];
   // pair (d_x psi, d_y psi)
@@ -531,6 +583,7 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
     }
   // forward x-FFT of both real products at once
   F::template run<-1>(v, lane, sm, tw);
+  }
   F::to_smem(v, lane, sm);
   fft_sync<C::TPF>();
   const size_t oplane = (size_t)gd.nh * N;
