@@ -18,6 +18,10 @@
    the GPU time per unit of physical time of the LES is compared with the
    DNS's.
 
+A network whose held-out loss is not below 0.9 (1 = no better than
+predicting the mean) is not applied: that LES runs as the hyperviscous
+fallback.
+
 The LES applies the network's tendencies only on the shells next to the
 cutoff, 2 k_c/3 <= k <= k_c (``band``, r2d3c_closure_set_band).  The subgrid
 transfer of a sharp cutoff acts there; on the large scales the network's
@@ -216,14 +220,18 @@ def train_network(ds, train_steps=3000, batch=32, lr=1e-3, seed=1):
                  "val_loss": float(np.mean(val)) if val else None}
 
 
-def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near_cutoff",), time_dns=True):
+def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near_cutoff",), time_dns=True,
+             val_loss=None, skill_gate=0.9):
     """Stage 3: from every held-out start, the plain coarse solver, the
     hyperviscous fallback and one LES per band rule (``bands``, see
     band_weights) advance les_steps CFL steps; spectra and fluxes averaged
     over the second half of every run and over the starts are compared with
     the filtered DNS's over its whole record.  With time_dns, the DNS
     continues over one LES run's mean physical time for the GPU-time gain
-    (of the first band rule's LES)."""
+    (of the first band rule's LES).  A network whose held-out loss
+    ``val_loss`` (standardised: 1 = predicting the mean) is not below
+    ``skill_gate`` has no skill to apply: its LES runs as the hyperviscous
+    fallback, the closure's stated fallback."""
     import torch
     cfg = ds["cfg"]
     nc, nu, hnu, omega, cfl = cfg["nc"], cfg["nu"], cfg["hnu"], cfg["omega"], cfg["cfl"]
@@ -240,9 +248,10 @@ def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near
             p.nu = p.nuv = nu * kc ** 2 / kc ** (2 * nn_) * 20.0
         models[name] = (p, None)
     pl = make_params(n=nc, nu=nu, nuv=nu, hnu=hnu, hnuv=hnu, nn=1, mm=2, nnv=1, mmv=2, omega=omega, iflow=0, cfl=cfl)
+    gated = val_loss is not None and not (val_loss < skill_gate)
     les_names = []
     for b in bands:
-        models[_rule_name(b)] = (pl, b)
+        models[_rule_name(b)] = (models["fallback"][0], None) if gated else (pl, b)
         les_names.append(_rule_name(b))
     spectra = {k: [] for k in models}
     fluxes = {k: [] for k in models}
@@ -264,7 +273,7 @@ def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near
             t0 = time.perf_counter()
             t_end = ds["snap_t"][si]
             for s in range(0, les_steps, spec_every):
-                if name in les_names:
+                if name in les_names and not gated:
                     t_end, _ = closure_advance(c, net, spec_every, DT_CFL, cfl)
                 else:
                     t_end, _ = c.advance(spec_every, DT_CFL, cfl)
@@ -285,7 +294,9 @@ def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near
     dns = {"n": cfg["nf"], "physical_time": T,
            "reference": f"filtered DNS spectra and fluxes averaged over all {len(ds['spec'])} snapshots"}
     les = {"n": nc, "steps": les_steps, "starts": nst, "gpu_s": {k: v / nst for k, v in t_les_gpu.items()},
-           "note": "gpu_s and physical_time per LES run (mean over starts)"}
+           "note": "gpu_s and physical_time per LES run (mean over starts)",
+           "network_applied": not gated,
+           "gate": f"held-out loss {val_loss} {'>=' if gated else '<'} {skill_gate}" if val_loss is not None else None}
     if time_dns:
         fine = ds["fine"]
         torch.cuda.synchronize()
@@ -336,7 +347,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
                      seed=seed, hnu=hnu, starts=starts)
     net, training = train_network(ds, train_steps=train_steps, batch=batch, lr=lr, seed=seed)
     ev = evaluate(ds, net, les_steps=les_steps, spec_every=spec_every, fallback_nn=fallback_nn,
-                  bands=(band,) + tuple(compare_bands))
+                  bands=(band,) + tuple(compare_bands), val_loss=training["val_loss"])
     name = _rule_name(band)
     err = {"les": ev["spectrum_error"][name], "plain": ev["spectrum_error"]["plain"],
            "fallback": ev["spectrum_error"]["fallback"]}

@@ -44,10 +44,11 @@ def test_optimiser_step_reaches_the_network(gpu):
     m = ClosureNet(H, W, B, seed=6)
     x = torch.randn((B, H, W, 8), device="cuda")
     y0 = m(x).detach().clone()
-    opt = torch.optim.SGD(m.parameters(), lr=0.5)
     loss = (m(x) ** 2).mean()
-    opt.zero_grad()
     loss.backward()
+    # a step that the linearisation says lowers the loss by 5%
+    g2 = float((m.params.grad ** 2).sum())
+    opt = torch.optim.SGD(m.parameters(), lr=0.05 * float(loss) / g2)
     opt.step()
     y1 = m(x).detach()
     assert float((y1 ** 2).mean()) < float((y0 ** 2).mean())
