@@ -23,6 +23,10 @@ def test_les_workflow_small(gpu):
     for name in ("les", "plain", "fallback"):
         e = r["spectrum_error"][name]
         assert all(math.isfinite(v) for v in e.values()), (name, e)
+    # a network without held-out skill is not applied: its LES is the fallback
+    assert r["les"]["network_applied"] == (tr["val_loss"] < 0.9)
+    if not r["les"]["network_applied"]:
+        assert r["spectrum_error"]["les"] == r["spectrum_error"]["fallback"]
 
 
 # A small case of the closure experiment: 512^2 DNS (nu = 1e-4, Omega = 1,
