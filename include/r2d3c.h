@@ -265,6 +265,12 @@ int r2d3c_closure_set_band(r2d3c_ctx* ctx, const float* w, int nshells);
    switched off on return. */
 int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
                           double* time, double* dt_last);
+/* The same with the network evaluated before every `every`-th step only (its
+   tendencies held for `every` steps; one CUDA graph of the evaluation and
+   `every` steps); nsteps must be a multiple of every.  every = 1 is
+   r2d3c_closure_advance.  No counterpart in the reference. */
+int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int every, int dt_mode,
+                                double cfl_or_dt, double* time, double* dt_last);
 
 /* ---- Regridding (regrid_slices.f90) ------------------------------------ */
 /* The reference's slice regridder applied to a whole field

@@ -179,10 +179,16 @@ def band_fit(net: CNN, X, Y, idx, n: int, batch: int = 8):
     return np.clip(w, 0.0, 1.0).astype(np.float32)
 
 
-def closure_advance(ctx, net: CNN, nsteps: int, dt_mode: int, cfl_or_dt: float):
+def closure_advance(ctx, net: CNN, nsteps: int, dt_mode: int, cfl_or_dt: float, every: int = 1):
     """nsteps LES steps of ctx with the network evaluated before every step
-    (one captured CUDA graph per step).  Returns (time, dt of the last step)."""
+    (``every`` > 1: before every every-th step, its tendencies held in
+    between; one captured CUDA graph per evaluation and its steps).
+    Returns (time, dt of the last step)."""
     t, dtl = C.c_double(), C.c_double()
-    check(load().r2d3c_closure_advance(ctx._h, net._h, nsteps, dt_mode, cfl_or_dt, C.byref(t), C.byref(dtl)),
-          "closure_advance")
+    if every == 1:
+        check(load().r2d3c_closure_advance(ctx._h, net._h, nsteps, dt_mode, cfl_or_dt, C.byref(t), C.byref(dtl)),
+              "closure_advance")
+    else:
+        check(load().r2d3c_closure_advance_every(ctx._h, net._h, nsteps, every, dt_mode, cfl_or_dt, C.byref(t),
+                                                 C.byref(dtl)), "closure_advance_every")
     return t.value, dtl.value

@@ -1133,9 +1133,15 @@ int r2d3c_closure_set_band(r2d3c_ctx* ctx, const float* w, int nshells) {
 
 int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
                           double* time, double* dt_last) {
+  return r2d3c_closure_advance_every(ctx, cnn, nsteps, 1, dt_mode, cfl_or_dt, time, dt_last);
+}
+
+int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int every, int dt_mode,
+                                double cfl_or_dt, double* time, double* dt_last) {
   API_BEGIN
   REQUIRE(ctx && cnn, "NULL argument");
   REQUIRE(nsteps >= 0, "nsteps must be >= 0");
+  REQUIRE(every >= 1 && nsteps % every == 0, "every must be >= 1 and divide nsteps");
   REQUIRE(dt_mode == R2D3C_DT_CFL || dt_mode == R2D3C_DT_FIXED, "bad dt_mode");
   REQUIRE(cfl_or_dt > 0.0 && std::isfinite(cfl_or_dt), "cfl_or_dt must be positive and finite");
   REQUIRE(ctx->p.iflow == 0 || ctx->p.iflow == 1, "the closure advance takes constant forcing (iflow 0 or 1)");
@@ -1179,12 +1185,15 @@ int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mod
   }
   try {
     if (dt_mode == R2D3C_DT_FIXED) e->set_dt(cfl_or_dt);
+    e->set_hook_every(every);
     e->advance(ctx->mc(), nsteps, dt_mode == R2D3C_DT_CFL, cfl_or_dt, nullptr);
   } catch (...) {
+    e->set_hook_every(1);
     e->set_step_hook(nullptr, 0);
     e->set_closure(nullptr, true);
     throw;
   }
+  e->set_hook_every(1);
   e->set_step_hook(nullptr, 0);
   e->set_closure(nullptr, true);
   if (time) *time = e->get_time();

@@ -131,6 +131,10 @@ class IEngine {
   // the captured graph (id != 0; id identifies the hook for the graph cache,
   // and id 0 removes it).
   virtual void set_step_hook(std::function<void(cudaStream_t)> hook, unsigned long long id) = 0;
+  // The hook runs before every k-th step only: advance() then replays one
+  // graph of the hook and k steps, and nsteps must be a multiple of k
+  // (constant forcing only).  k = 1 is the default.
+  virtual void set_hook_every(int k) = 0;
   virtual void rand_force(const RandForceHost f[2]) = 0;
   // One RK4 step.  cfl_mode: dt from the CFL condition of the current state
   // (fused into the first substep), else the dt already set.  add_time:

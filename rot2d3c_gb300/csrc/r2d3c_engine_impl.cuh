@@ -451,7 +451,10 @@ class EngineT final : public IEngine {
       sync();  // seq goes out of scope
     }
     upload_coefs(mc, cfl);
-    GraphKey key{cfl_mode, rf != nullptr, closure_on_, band_nw_ > 0, hook_ ? hook_id_ : 0ull};
+    const int every = hook_ ? hook_every_ : 1;
+    if (nsteps % every != 0) throw Error(kEINVAL, "nsteps must be a multiple of the hook interval");
+    if (every > 1 && rf) throw Error(kEINVAL, "a hook interval above 1 takes constant forcing");
+    GraphKey key{cfl_mode, rf != nullptr, closure_on_, band_nw_ > 0, hook_ ? hook_id_ : 0ull, every};
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
@@ -460,7 +463,7 @@ class EngineT final : public IEngine {
       cuda_check(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal), "BeginCapture");
       try {
         if (hook_) hook_(st_);
-        enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr);
+        for (int k = 0; k < every; ++k) enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr);
       } catch (...) {
         cudaStreamEndCapture(st_, &g);
         if (g) cudaGraphDestroy(g);
@@ -473,10 +476,14 @@ class EngineT final : public IEngine {
       launches_ = before;
       gkey_ = key;
     }
-    for (int s = 0; s < nsteps; ++s) {
+    for (int s = 0; s < nsteps; s += every) {
       cuda_check(cudaGraphLaunch(graph_, st_), "GraphLaunch");
       launches_ += graph_launches_;
     }
+  }
+  void set_hook_every(int k) override {
+    if (k < 1) throw Error(kEINVAL, "hook interval must be >= 1");
+    hook_every_ = k;
   }
 
   void initial_condition_phys(const std::vector<IcModeHost>& modes) override {
@@ -551,10 +558,13 @@ class EngineT final : public IEngine {
   struct GraphKey {
     bool cfl_mode = false, rf = false, closure = false, band = false;
     unsigned long long hook = 0;
+    int every = 1;  // steps per graph (the hook's interval)
     bool same(const GraphKey& o) const {
-      return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure && band == o.band && hook == o.hook;
+      return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure && band == o.band && hook == o.hook &&
+             every == o.every;
     }
   };
+  int hook_every_ = 1;
   static bool batched(int p) { return p <= P_C2; }  // ps, vz, fp, fz, c1, c2
 
  public:

@@ -154,3 +154,42 @@ def test_graph_captured_les_steps_equal_the_step_by_step_loop(gpu, prec, band):
         b.advance(2, mode, val)
         for u, v in zip(a.get_state(), b.get_state()):
             np.testing.assert_array_equal(u, v)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_network_every_second_step_equals_the_step_by_step_loop(gpu, prec):
+    """r2d3c_closure_advance_every with every = 2: the network evaluated
+    before every second step and its tendencies held for two steps, in one
+    graph per pair of steps; bit-identical to the same schedule made one
+    call at a time."""
+    import torch
+    from rot2d3c_gb300.closure import CNN, closure_advance, closure_inputs, set_tendency
+    n = 32
+    _, cp = params(n, omega=1.0, nu=2e-3, nuv=2e-3, hnu=0.1, hnuv=0.1, iflow=0)
+    g, ps, vz = random_state(n, 51, amp=20.0)
+    fp, fz = random_forcing(g, 52, 2.0, 4.0)
+    net = CNN(n, n, 1, 9)
+    net.set_normalization(np.zeros(8), np.full(8, 50.0), np.zeros(2), np.full(2, 5.0))
+    for mode, val in ((gpu.DT_CFL, 0.4), (gpu.DT_FIXED, 1e-3)):
+        a = gpu.Context(cp, prec)
+        b = gpu.Context(cp, prec)
+        for c in (a, b):
+            c.set_state(ps, vz)
+            c.set_forcing(fp, fz)
+            c.set_time(0.0)
+        x = torch.empty((1, n, n, 8), dtype=torch.float32, device="cuda")
+        t = torch.empty((1, n, n, 2), dtype=torch.float32, device="cuda")
+        for s in range(6):
+            if s % 2 == 0:
+                closure_inputs(a, x[0])
+                net.forward(x, 1, t)
+                set_tendency(a, t[0])
+            ta, _ = a.advance(1, mode, val)
+        set_tendency(a, None)
+        tb, _ = closure_advance(b, net, 4, mode, val, every=2)
+        tb, _ = closure_advance(b, net, 2, mode, val, every=2)
+        assert ta == tb
+        for u, v in zip(a.get_state(), b.get_state()):
+            np.testing.assert_array_equal(u, v)
+    with pytest.raises(gpu.R2D3CError):
+        closure_advance(b, net, 3, gpu.DT_FIXED, 1e-3, every=2)
