@@ -26,7 +26,8 @@ constexpr int kOK = 0, kEINVAL = -1, kECUDA = -2, kENOMEM = -3, kETIMEOUT = -4, 
 void cuda_check(cudaError_t e, const char* what);
 
 // Spectral planes: complex [kx][ky], (n/2+1) x n.
-enum Plane : int { P_PS = 0, P_VZ, P_FP, P_FZ, P_C1, P_C2, P_W1, P_W2, P_B5, P_B6, P_T5, P_T6, P_COUNT };
+// (C1, C2 and C3, C4: the substep state, ping-ponged between the substeps)
+enum Plane : int { P_PS = 0, P_VZ, P_FP, P_FZ, P_C1, P_C2, P_C3, P_C4, P_W1, P_W2, P_B5, P_B6, P_T5, P_T6, P_COUNT };
 // Real planes: [y][x], n x n.
 enum RPlane : int { R_1 = 0, R_2, R_3, R_COUNT };
 

@@ -565,7 +565,7 @@ class EngineT final : public IEngine {
     }
   };
   int hook_every_ = 1;
-  static bool batched(int p) { return p <= P_C2; }  // ps, vz, fp, fz, c1, c2
+  static bool batched(int p) { return p <= P_C4; }  // ps, vz, fp, fz, c1 .. c4
 
  public:
   void set_step_hook(std::function<void(cudaStream_t)> hook, unsigned long long id) override {
@@ -857,17 +857,23 @@ class EngineT final : public IEngine {
     if (nb_ > 1 && (rf_mode != 0 || ci_on_)) throw Error(kEINVAL, "batched runs take constant forcing");
     cpx<T>* ps = pbase_[P_PS];
     cpx<T>* vz = pbase_[P_VZ];
-    cpx<T>* c1 = pbase_[P_C1];
-    cpx<T>* c2 = pbase_[P_C2];
     const unsigned rb = (unsigned)((nb_ + 31) / 32);
+    // The substep state moves ps -> C1 -> C3 -> C1 -> ps (and vz -> C2 -> C4
+    // -> C2 -> vz): no substep updates its own input in place, so pass C may
+    // split a column pair's C1 and C2 updates over two CTAs (the last
+    // substep writes ps, vz, which only the element's own thread reads).
     for (int o = 4; o >= 1; --o) {
-      const cpx<T>* in1 = o == 4 ? ps : c1;
-      const cpx<T>* in2 = o == 4 ? vz : c2;
-      cpx<T>* out1 = o == 1 ? ps : c1;
-      cpx<T>* out2 = o == 1 ? vz : c2;
+      const int pin1 = o == 4 ? P_PS : o == 2 ? P_C3 : P_C1;
+      const int pin2 = o == 4 ? P_VZ : o == 2 ? P_C4 : P_C2;
+      const int pout1 = o == 1 ? P_PS : o == 3 ? P_C3 : P_C1;
+      const int pout2 = o == 1 ? P_VZ : o == 3 ? P_C4 : P_C2;
+      const cpx<T>* in1 = pbase_[pin1];
+      const cpx<T>* in2 = pbase_[pin2];
+      cpx<T>* out1 = pbase_[pout1];
+      cpx<T>* out2 = pbase_[pout2];
       if (ci_on_) {  // const_inj every substep (Rot2D3C.para.f90:565-569)
-        enqueue_const_inj(in1, o == 4 ? P_PS : P_C1, P_FP, 1, ci_fp0_);
-        enqueue_const_inj(in2, o == 4 ? P_VZ : P_C2, P_FZ, 0, ci_fz0_);
+        enqueue_const_inj(in1, pin1, P_FP, 1, ci_fp0_);
+        enqueue_const_inj(in2, pin2, P_FZ, 0, ci_fz0_);
       }
       timed(0, [&] { launch_passA(in1, in2, tf_, nb_); });
       if (o == 4 && cfl_mode) {
@@ -1047,7 +1053,8 @@ class EngineT final : public IEngine {
         auto k = k_passC<T, N>;
         const int groups = (gd_.M + NT - 1) / NT;
         const int g = gc_ ? gc_ : C::G;  // groups per CTA: autotuned
-        const dim3 grid((groups + g - 1) / g, nb);
+        // the C1 and C2 updates of a column pair in one CTA or two (autotuned)
+        const dim3 grid((groups + g - 1) / g, nb, kChunkC<T, N> ? fc_ : 1);
         k<<<grid, C::TPF * g, g * PassSmem<T, N>::GROUP_ELEMS * sizeof(cpx<T>), st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ],
                                                            pbase_[P_FP], pbase_[P_FZ], c1out, c2out, gd_, d_sc_,
                                                            scal_base_, o, tw_, batch(), t5, t6);
@@ -1155,14 +1162,17 @@ class EngineT final : public IEngine {
   }
   // R2D3C_GROUPS="ga,fa,gb,gc" fixes the groups per CTA of passes A, B, C
   // and pass A's field chunks (0 for a group count: the config's G)
-  static void forced_groups(int G_A, int G_B, int G_C, int out[4]) {
+  static void forced_groups(int G_A, int G_B, int G_C, int out[5]) {
     out[0] = out[2] = out[3] = -1;
     out[1] = -1;
+    out[4] = -1;
     const char* e = std::getenv("R2D3C_GROUPS");
     if (!e) return;
-    int v[4];
-    if (std::sscanf(e, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]) != 4)
-      throw Error(kEINVAL, "R2D3C_GROUPS must be ga,fa,gb,gc");
+    int v[5] = {0, 0, 0, 0, -1};
+    const int got = std::sscanf(e, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]);
+    if (got != 4 && got != 5) throw Error(kEINVAL, "R2D3C_GROUPS must be ga,fa,gb,gc[,cc]");
+    if (got == 5 && v[4] != 1 && v[4] != 2) throw Error(kEINVAL, "R2D3C_GROUPS: pass C chunks must be 1 or 2");
+    out[4] = got == 5 ? v[4] : -1;
     auto group_ok = [](int g, int G) { return g == 0 || (g >= 1 && g <= G && (g & (g - 1)) == 0); };
     if (!group_ok(v[0], G_A) || !group_ok(v[2], G_B) || !group_ok(v[3], G_C) ||
         !(v[1] == 1 || v[1] == 2 || v[1] == 3 || v[1] == 6))
@@ -1226,24 +1236,37 @@ class EngineT final : public IEngine {
         cuda_check(cudaMemsetAsync(pb_, 0, sizeof(cpx<T>) * 2 * S_ * nb_, st_), "memset");
         cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
         coefs_valid_ = false;
-        std::vector<std::pair<int, int>> cands;
-        for (int g = GB; g >= 1; g /= 2) cands.push_back({0, g});
+        struct CandC {
+          int mode, grid, chunks;
+        };
+        std::vector<CandC> cands;
+        for (int g = GB; g >= 1; g /= 2) {
+          cands.push_back({0, g, 1});
+          if constexpr (kChunkC<T, N>) cands.push_back({0, g, 2});
+        }
         if constexpr (kPipeC<T, N>) {
-          cands.push_back({1, pipec_ctas_});
-          if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2});
+          cands.push_back({1, pipec_ctas_, 1});
+          if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2, 1});
         }
         cpx<T>* c1 = planes_[P_C1];
         cpx<T>* c2 = planes_[P_C2];
+        cpx<T>* c3 = planes_[P_C3];
+        cpx<T>* c4 = planes_[P_C4];
         const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
-          passc_mode_ = cands[i].first;
-          pipec_grid_ = cands[i].first ? cands[i].second : 0;
-          gc_ = cands[i].first ? GB : cands[i].second;
-          launch_passC(c1, c2, c1, c2, 4, nb_);
+          passc_mode_ = cands[i].mode;
+          pipec_grid_ = cands[i].mode ? cands[i].grid : 0;
+          gc_ = cands[i].mode ? GB : cands[i].grid;
+          fc_ = cands[i].chunks;
+          launch_passC(c1, c2, c3, c4, 4, nb_);
         });
         tune_c_.clear();
-        for (size_t i = 0; i < cands.size(); ++i) tune_c_.push_back({cands[i].first, cands[i].second, us[i]});
-        cuda_check(cudaMemsetAsync(planes_[P_C1], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
-        cuda_check(cudaMemsetAsync(planes_[P_C2], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
+        for (size_t i = 0; i < cands.size(); ++i) {
+          TuneRec r{cands[i].mode, cands[i].grid, us[i]};
+          r.chunks = cands[i].chunks;
+          tune_c_.push_back(r);
+        }
+        for (int p : {P_C1, P_C2, P_C3, P_C4})
+          cuda_check(cudaMemsetAsync(planes_[p], 0, sizeof(cpx<T>) * S_ * nb_, st_), "memset");
       }
       launches_ = saved;
     });
@@ -1263,7 +1286,7 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       constexpr int GA = CfgA<T, N>::G;
       constexpr int GB = Cfg<T, N, PassNT<T, N>::value>::G;
-      int forced[4];
+      int forced[5];
       forced_groups(GA, GB, GB, forced);
       auto argmin = [](const std::vector<TuneRec>& t, const std::function<bool(const TuneRec&)>& ok) {
         size_t k = t.size();
@@ -1331,9 +1354,12 @@ class EngineT final : public IEngine {
         mode = t[pick].mode;
         grid = mode ? t[pick].grid : 0;
         groups = forced_g >= 0 ? (forced_g ? forced_g : GB) : t[pick0].grid;
+        return pick0;
       };
       pick_bc(tune_, "R2D3C_PASSB", "per_row_pair", forced[2], passb_mode_, pipeb_grid_, gb_);
-      pick_bc(tune_c_, "R2D3C_PASSC", "per_column_pair", forced[3], passc_mode_, pipec_grid_, gc_);
+      const size_t c0 = pick_bc(tune_c_, "R2D3C_PASSC", "per_column_pair", forced[3], passc_mode_, pipec_grid_, gc_);
+      fc_ = forced[4] > 0 ? forced[4] : (c0 < tune_c_.size() ? tune_c_[c0].chunks : 1);
+      if (!kChunkC<T, N>) fc_ = 1;
     });
   }
   void set_plan_policy(int policy) override {
@@ -1372,12 +1398,12 @@ class EngineT final : public IEngine {
         snprintf(b, sizeof b, "%s{\"variant\": \"persistent\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
                  tune_c_[i].grid, (double)tune_c_[i].us);
       else
-        snprintf(b, sizeof b, "%s{\"variant\": \"per_column_pair\", \"groups\": %d, \"us\": %.2f}", i ? ", " : "",
-                 tune_c_[i].grid, (double)tune_c_[i].us);
+        snprintf(b, sizeof b, "%s{\"variant\": \"per_column_pair\", \"groups\": %d, \"chunks\": %d, \"us\": %.2f}",
+                 i ? ", " : "", tune_c_[i].grid, tune_c_[i].chunks, (double)tune_c_[i].us);
       r += b;
     }
-    snprintf(b, sizeof b, "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d}",
-             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_);
+    snprintf(b, sizeof b, "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d, \"chunks_c\": %d}",
+             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_, fc_);
     return r + b;
   }
 
@@ -1419,11 +1445,13 @@ class EngineT final : public IEngine {
   int sms_ = 0;         // SMs of the device
   int policy_ = 0;      // plan policy (choose_plan)
   int ga_ = 0, fa_ = 1;  // pass A: groups per CTA (0: the config's G), field chunks (autotuned)
+  int fc_ = 1;           // pass C: CTAs per column pair (1 or 2, autotuned)
   int gb_ = 0, gc_ = 0;  // passes B, C one CTA per row / column pair: groups per CTA (autotuned)
   struct TuneRec {
     int mode, grid;  // pass A: groups, field chunks; B, C: variant, CTAs or groups
     float us;
-    int radix = 0;  // pass A: the transform radix
+    int radix = 0;   // pass A: the transform radix
+    int chunks = 1;  // pass C: CTAs per column pair
   };
   // pass A radix chosen per (precision, n), shared by the engines of a process
   static std::map<int, int>& radix_cache() {

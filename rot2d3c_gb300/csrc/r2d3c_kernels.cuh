@@ -851,24 +851,39 @@ __device__ __forceinline__ void rk_load(RkIn<T>& r, size_t idx, const cpx<T>* c1
   r.g0 = fz[idx];
 }
 
-// New C1, C2 of one element (Rot2D3C.para.f90:580-599); zero outside the
-// retained disc and at k = 0.
+// New C1 (rk_apply1) and C2 (rk_apply2) of one element
+// (Rot2D3C.para.f90:580-599); zero outside the retained disc and at k = 0.
+// The two are independent: C1 needs C2's input (the Coriolis term 2 Omega
+// d_y C2) and [psi, -k^2 psi], C2 needs C1's input and [psi, vz].
 template <typename T>
-__device__ __forceinline__ void rk_apply(const RkIn<T>& r, const cpx<T> c5, const cpx<T> c6, int kyi, int k2,
-                                         const StepCoef& sc, T tmp1, cpx<T>& n1, cpx<T>& n2) {
-  const T nu = (T)sc.nu, hnu = (T)sc.hnu, nuv = (T)sc.nuv, hnuv = (T)sc.hnuv, w2 = (T)sc.w2;
+__device__ __forceinline__ cpx<T> rk_apply1(const RkIn<T>& r, const cpx<T> c5, int kyi, int k2, const StepCoef& sc,
+                                            T tmp1) {
+  const T nu = (T)sc.nu, hnu = (T)sc.hnu, w2 = (T)sc.w2;
   const T kyf = (T)kyi, ka2 = (T)k2;
-  const cpx<T> C3 = mkc<T>(-kyf * r.a1.y, kyf * r.a1.x);  // derivk2(C1,C3,2)
   const cpx<T> C4 = mkc<T>(-kyf * r.a2.y, kyf * r.a2.x);  // derivk2(C2,C4,2)
   const T tmp2 = (T)1 / ka2;
   const T tmp3 = (T)1 + (nu * powi(ka2, sc.nn) + hnu * powi(tmp2, sc.mm)) * tmp1;
   const T u1x = r.p0.x + ((-c5.x + w2 * C4.x) * tmp2 + r.f0.x) * tmp1;
   const T u1y = r.p0.y + ((-c5.y + w2 * C4.y) * tmp2 + r.f0.y) * tmp1;
-  n1 = mkc<T>(u1x / tmp3, u1y / tmp3);
+  return mkc<T>(u1x / tmp3, u1y / tmp3);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> rk_apply2(const RkIn<T>& r, const cpx<T> c6, int kyi, int k2, const StepCoef& sc,
+                                            T tmp1) {
+  const T nuv = (T)sc.nuv, hnuv = (T)sc.hnuv, w2 = (T)sc.w2;
+  const T kyf = (T)kyi, ka2 = (T)k2;
+  const cpx<T> C3 = mkc<T>(-kyf * r.a1.y, kyf * r.a1.x);  // derivk2(C1,C3,2)
+  const T tmp2 = (T)1 / ka2;
   const T tmp3v = (T)1 + (nuv * powi(ka2, sc.nnv) + hnuv * powi(tmp2, sc.mmv)) * tmp1;
   const T u2x = r.v0.x + (c6.x + w2 * C3.x + r.g0.x) * tmp1;
   const T u2y = r.v0.y + (c6.y + w2 * C3.y + r.g0.y) * tmp1;
-  n2 = mkc<T>(u2x / tmp3v, u2y / tmp3v);
+  return mkc<T>(u2x / tmp3v, u2y / tmp3v);
+}
+template <typename T>
+__device__ __forceinline__ void rk_apply(const RkIn<T>& r, const cpx<T> c5, const cpx<T> c6, int kyi, int k2,
+                                         const StepCoef& sc, T tmp1, cpx<T>& n1, cpx<T>& n2) {
+  n1 = rk_apply1<T>(r, c5, kyi, k2, sc, tmp1);
+  n2 = rk_apply2<T>(r, c6, kyi, k2, sc, tmp1);
 }
 
 // L2 prefetch (cp.async.bulk.prefetch, no completion to wait for) of the
@@ -906,12 +921,17 @@ __device__ __forceinline__ void passC_update_pairs(cpx<T>* sm, const cpx<T>* hol
                                                    const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out,
                                                    const DevGrid& gd, const StepCoef& sc, T tmp1,
                                                    const cpx<T>* __restrict__ tau5,
-                                                   const cpx<T>* __restrict__ tau6) {
+                                                   const cpx<T>* __restrict__ tau6, int chunk = -1) {
+  // chunk -1: both outputs; 0: C1 only (v and hold hold the [psi,-k^2 psi]
+  // columns); 1: C2 only (v holds the [psi, vz] columns)
+  const bool do1 = chunk != 1, do2 = chunk != 0;
   cpx<T>* c6s = sm;
+  if (do2) {
 #pragma unroll
-  for (int t = 0; t < NT; ++t)
+    for (int t = 0; t < NT; ++t)
 #pragma unroll
-    for (int q = 0; q < E; ++q) c6s[t * N + lane + q * TPF] = v[t][q];
+      for (int q = 0; q < E; ++q) c6s[t * N + lane + q * TPF] = v[t][q];
+  }
   __syncthreads();
   const int L = gd.L;
   const int lo_pairs = L / 2 + 1;       // pairs p = 0 .. L/2 hold rows 0 .. L
@@ -943,12 +963,12 @@ __device__ __forceinline__ void passC_update_pairs(cpx<T>* sm, const cpx<T>* hol
       }
       if (any) {
         const size_t idx = (size_t)col[b] * N + j0[b];
-        a1[b] = ld4(c1in, idx);
-        a2[b] = ld4(c2in, idx);
-        p0[b] = ld4(ps, idx);
-        f0[b] = ld4(fp, idx);
-        v0[b] = ld4(vz, idx);
-        g0[b] = ld4(fz, idx);
+        if (do2) a1[b] = ld4(c1in, idx);
+        if (do1) a2[b] = ld4(c2in, idx);
+        if (do1) p0[b] = ld4(ps, idx);
+        if (do1) f0[b] = ld4(fp, idx);
+        if (do2) v0[b] = ld4(vz, idx);
+        if (do2) g0[b] = ld4(fz, idx);
       }
     }
 #pragma unroll
@@ -963,32 +983,41 @@ __device__ __forceinline__ void passC_update_pairs(cpx<T>* sm, const cpx<T>* hol
         if (!in[b][h]) return;
         const int ky = ky_of(j0[b] + h, N), k2 = col[b] * col[b] + ky * ky;
         RkIn<T> r;
-        r.a1 = h ? mkc<T>(a1[b].z, a1[b].w) : mkc<T>(a1[b].x, a1[b].y);
-        r.a2 = h ? mkc<T>(a2[b].z, a2[b].w) : mkc<T>(a2[b].x, a2[b].y);
-        r.p0 = h ? mkc<T>(p0[b].z, p0[b].w) : mkc<T>(p0[b].x, p0[b].y);
-        r.f0 = h ? mkc<T>(f0[b].z, f0[b].w) : mkc<T>(f0[b].x, f0[b].y);
-        r.v0 = h ? mkc<T>(v0[b].z, v0[b].w) : mkc<T>(v0[b].x, v0[b].y);
-        r.g0 = h ? mkc<T>(g0[b].z, g0[b].w) : mkc<T>(g0[b].x, g0[b].y);
-        cpx<T> c5 = hold[t * N + j0[b] + h], c6 = c6s[t * N + j0[b] + h];
-        if (tau5) {  // learned subgrid tendencies of the two brackets
-          const cpx<T> u = tau5[idx + h], w = tau6[idx + h];
-          c5 = mkc<T>(c5.x + u.x, c5.y + u.y);
-          c6 = mkc<T>(c6.x + w.x, c6.y + w.y);
+        if (do1) {
+          r.a2 = h ? mkc<T>(a2[b].z, a2[b].w) : mkc<T>(a2[b].x, a2[b].y);
+          r.p0 = h ? mkc<T>(p0[b].z, p0[b].w) : mkc<T>(p0[b].x, p0[b].y);
+          r.f0 = h ? mkc<T>(f0[b].z, f0[b].w) : mkc<T>(f0[b].x, f0[b].y);
+          cpx<T> c5 = hold[t * N + j0[b] + h];
+          if (tau5) {  // learned subgrid tendency of the first bracket
+            const cpx<T> u = tau5[idx + h];
+            c5 = mkc<T>(c5.x + u.x, c5.y + u.y);
+          }
+          n1 = rk_apply1<T>(r, c5, ky, k2, sc, tmp1);
         }
-        rk_apply<T>(r, c5, c6, ky, k2, sc, tmp1, n1, n2);
+        if (do2) {
+          r.a1 = h ? mkc<T>(a1[b].z, a1[b].w) : mkc<T>(a1[b].x, a1[b].y);
+          r.v0 = h ? mkc<T>(v0[b].z, v0[b].w) : mkc<T>(v0[b].x, v0[b].y);
+          r.g0 = h ? mkc<T>(g0[b].z, g0[b].w) : mkc<T>(g0[b].x, g0[b].y);
+          cpx<T> c6 = c6s[t * N + j0[b] + h];
+          if (tau5) {  // learned subgrid tendency of the second bracket
+            const cpx<T> w = tau6[idx + h];
+            c6 = mkc<T>(c6.x + w.x, c6.y + w.y);
+          }
+          n2 = rk_apply2<T>(r, c6, ky, k2, sc, tmp1);
+        }
       };
       cpx<T> n10, n20, n11, n21;
       row(0, n10, n20);
       row(1, n11, n21);
       if (keep[b][0] && keep[b][1]) {
-        *reinterpret_cast<F4*>(c1out + idx) = make_float4(n10.x, n10.y, n11.x, n11.y);
-        *reinterpret_cast<F4*>(c2out + idx) = make_float4(n20.x, n20.y, n21.x, n21.y);
+        if (do1) *reinterpret_cast<F4*>(c1out + idx) = make_float4(n10.x, n10.y, n11.x, n11.y);
+        if (do2) *reinterpret_cast<F4*>(c2out + idx) = make_float4(n20.x, n20.y, n21.x, n21.y);
       } else if (keep[b][0]) {
-        c1out[idx] = n10;
-        c2out[idx] = n20;
+        if (do1) c1out[idx] = n10;
+        if (do2) c2out[idx] = n20;
       } else {
-        c1out[idx + 1] = n11;
-        c2out[idx + 1] = n21;
+        if (do1) c1out[idx + 1] = n11;
+        if (do2) c2out[idx + 1] = n21;
       }
     }
   }
@@ -1030,13 +1059,23 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
     const int lane = lane0;
     const cpx<T>* src = lane == 0 ? c1in : lane == 1 ? c2in : lane == 2 ? ps : lane == 3 ? vz
                       : lane == 4 ? fp : lane == 5 ? fz : lane == 6 ? tau5 : tau6;
+    // with two chunks each CTA needs half of them: z = 0 the C1 update's
+    // (c2in, ps, fp, tau5), z = 1 the C2 update's (c1in, vz, fz, tau6)
+    const int user = lane < 2 ? 1 - lane : (lane & 1);  // the chunk that reads src
+    const bool need = gridDim.z == 1 || !(sizeof(T) == 4 && HOLD) || (int)blockIdx.z == user;
     const int ncol = min(NT, gd.M - kx0);
-    if (src && ncol > 0) prefetch_columns_l2<T>(src + (size_t)kx0 * N, ncol, N, gd.L);
+    if (src && need && ncol > 0) prefetch_columns_l2<T>(src + (size_t)kx0 * N, ncol, N, gd.L);
   }
   cpx<T> v[NT][C::E];
   cpx<T> c5r[HOLD ? 1 : NT][C::E];
+  // gridDim.z = 2 splits a column pair's work over two CTAs (FP32 grids with
+  // the held c5): z = 0 transforms [psi,-k^2 psi] and updates C1, z = 1
+  // transforms [psi, vz] and updates C2; the arithmetic per element is the
+  // same as with one CTA (the launch autotuner chooses)
+  const int chunk = (HOLD && sizeof(T) == 4 && gridDim.z > 1) ? (int)blockIdx.z : -1;
 #pragma unroll 1
   for (int pl = 0; pl < 2; ++pl) {
+    if (chunk >= 0 && pl != chunk) continue;
     // the loop-invariant addresses of the transform are recomputed per
     // iteration from an opaque copy of the lane index instead of being
     // hoisted out of the loop and held in registers across it
@@ -1086,7 +1125,7 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   const T tmp1 = (T)(scal[blockIdx.y * kScalStride] / (double)o);  // :581
   if constexpr (HOLD && sizeof(T) == 4) {
     passC_update_pairs<T, N, NT, C::E, C::TPF>(sm, hold, v, lane, kx0, c1in, c2in, ps, vz, fp, fz, c1out, c2out, gd,
-                                                sc, tmp1, tau5, tau6);
+                                                sc, tmp1, tau5, tau6, chunk);
   } else if constexpr (HOLD) {
     // c6 joins c5 in shared memory (the transform buffer is free after the
     // last transform; each thread reads back only what it wrote), and the
@@ -1185,6 +1224,10 @@ struct PipeC {
   // transform buffers, held c5 (2 columns), one staged plane (2 columns)
   static constexpr size_t SMEM = (size_t)2 * F::SMEM_ELEMS * sizeof(float2) + (size_t)4 * N * sizeof(float2);
 };
+// pass C may split a column pair's C1 and C2 updates over two CTAs (gridDim.z
+// = 2) where it holds c5 in shared memory and updates row pairs (FP32)
+template <typename T, int N>
+constexpr bool kChunkC = sizeof(T) == 4 && PassSmem<T, N>::HOLD;
 template <typename T, int N>
 constexpr bool kPipeC = sizeof(T) == 4 && PassNT<T, N>::value == 2 && PassSmem<T, N>::HOLD &&
                         PipeC<N>::THREADS >= 64 && PipeC<N>::THREADS <= 512;

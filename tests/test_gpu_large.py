@@ -99,10 +99,14 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     assert all(r["us"] > 0 for r in rep["pass_c"]) and rep["chosen_c"] in ("per_column_pair", "persistent")
     c.destroy()
     out = []
-    for mb, mc in (("per_row_pair", "per_column_pair"), ("persistent", "persistent"),
-                   ("persistent", "per_column_pair")):
+    for mb, mc, groups in (("per_row_pair", "per_column_pair", None), ("persistent", "persistent", None),
+                           ("persistent", "per_column_pair", None), ("persistent", "per_column_pair", "0,1,0,0,2")):
         monkeypatch.setenv("R2D3C_PASSB", mb)
         monkeypatch.setenv("R2D3C_PASSC", mc)
+        if groups:
+            monkeypatch.setenv("R2D3C_GROUPS", groups)
+        else:
+            monkeypatch.delenv("R2D3C_GROUPS", raising=False)
         c = gpu.Context(cp, 1)
         assert c.plan_report()["chosen"] == mb and c.plan_report()["chosen_c"] == mc
         c.set_state(ps, vz)
@@ -125,7 +129,7 @@ def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
     shapes only: every forced choice steps to the same bits as the tuned one."""
     cp, ps, vz, fp, fz = _case(n, 5)
     out, reps = [], []
-    for forced in (None, "1,6,1,1", "0,1,0,0", "2,3,1,2"):
+    for forced in (None, "1,6,1,1", "0,1,0,0", "2,3,1,2", "0,1,0,1,2", "1,2,1,2,2"):
         if forced is None:
             monkeypatch.delenv("R2D3C_GROUPS", raising=False)
         else:
@@ -142,10 +146,15 @@ def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
         c.destroy()
     assert reps[1]["groups_a"] == 1 and reps[1]["field_chunks_a"] == 6 and reps[1]["groups_b"] == 1
     assert reps[3]["field_chunks_a"] == 3
+    # pass C's C1 and C2 updates split over two CTAs per column pair (FP32)
+    assert reps[4]["chunks_c"] == (2 if prec == 1 else 1) and reps[5]["groups_c"] == 2
     for o in out[1:]:
         for u, v in zip(out[0], o):
             np.testing.assert_array_equal(u, v)
     monkeypatch.setenv("R2D3C_GROUPS", "3,1,1,1")
+    with pytest.raises(gpu.R2D3CError):
+        gpu.Context(cp, prec)
+    monkeypatch.setenv("R2D3C_GROUPS", "0,1,0,0,3")
     with pytest.raises(gpu.R2D3CError):
         gpu.Context(cp, prec)
 
