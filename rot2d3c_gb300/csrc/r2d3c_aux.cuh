@@ -300,21 +300,19 @@ __device__ __forceinline__ double dec_ordered(unsigned long long e) {
 }
 
 // one thread per run r: enc, scal at r * kScalStride, coefficients c[r]
-// dt of one run from its CFL maximum (and time += dt with add_time)
-__device__ __forceinline__ void cfl_dt_one(const unsigned long long* __restrict__ enc, const CflCoef& c,
-                                           double* scal, int add_time) {
+static __global__ void k_cfl_dt(const unsigned long long* __restrict__ enc, const CflCoef* __restrict__ cc,
+                                double* scal, int add_time, int nruns) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nruns) return;
+  enc += r * kScalStride;
+  scal += r * kScalStride;
+  const CflCoef c = cc[r];
   const double m = dec_ordered(enc[0]);
   const double tmp = __ddiv_rn(sqrt(m), c.nrm);
   const double den = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(c.kcut, tmp), c.nuk), c.nuvk), c.w2);
   const double dt = __ddiv_rn(c.cfl, den);
   scal[0] = dt;
   if (add_time) scal[1] = __dadd_rn(scal[1], dt);
-}
-static __global__ void k_cfl_dt(const unsigned long long* __restrict__ enc, const CflCoef* __restrict__ cc,
-                                double* scal, int add_time, int nruns) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nruns) return;
-  cfl_dt_one(enc + r * kScalStride, cc[r], scal + r * kScalStride, add_time);
 }
 
 // one device scalar set from a kernel parameter (no host buffer to keep

@@ -14,7 +14,6 @@
 
 #include "r2d3c_aux.cuh"
 #include "r2d3c_engine.h"
-#include "r2d3c_small.cuh"
 
 namespace r2d3c {
 
@@ -856,10 +855,6 @@ class EngineT final : public IEngine {
   // const_inj are single-run features.
   void enqueue_step(bool cfl_mode, bool add_time, int rf_mode, const RandForceHost* rf) {
     if (nb_ > 1 && (rf_mode != 0 || ci_on_)) throw Error(kEINVAL, "batched runs take constant forcing");
-    if (small_on_ && rf_mode == 0 && !ci_on_ && nb_ == 1) {  // (the kernel clears the CFL maximum itself)
-      launch_small(cfl_mode, add_time);
-      return;
-    }
     cpx<T>* ps = pbase_[P_PS];
     cpx<T>* vz = pbase_[P_VZ];
     const unsigned rb = (unsigned)((nb_ + 31) / 32);
@@ -1073,37 +1068,6 @@ class EngineT final : public IEngine {
   void set_kernel_attrs() {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
-      small_ok_ = false;
-      if constexpr (SmallStep<T, N>::OK) {
-        using SS = SmallStep<T, N>;
-        // a cluster of 16 CTAs (non-portable) where the device runs one, else 8
-        if (full_ && nb_ == 1) {
-          auto k = k_step_small<T, N>;
-          set_smem_attr(k, SS::SMEM);
-          cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
-                     "cudaFuncSetAttribute(non-portable cluster)");
-          for (int ncl : {16, 8}) {
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(ncl, 1, 1);
-            cfg.blockDim = dim3(SS::THREADS, 1, 1);
-            cfg.dynamicSmemBytes = SS::SMEM;
-            cudaLaunchAttribute at[1];
-            at[0].id = cudaLaunchAttributeClusterDimension;
-            at[0].val.clusterDim.x = ncl;
-            at[0].val.clusterDim.y = 1;
-            at[0].val.clusterDim.z = 1;
-            cfg.attrs = at;
-            cfg.numAttrs = 1;
-            int nclusters = 0;
-            if (cudaOccupancyMaxActiveClusters(&nclusters, k, &cfg) == cudaSuccess && nclusters >= 1) {
-              small_ncl_ = ncl;
-              small_ok_ = true;
-              break;
-            }
-            cudaGetLastError();
-          }
-        }
-      }
       constexpr size_t sm = Cfg<T, N>::SMEM;
       set_smem_attr(k_colfft<T, N, -1>, sm);
       set_smem_attr(k_colfft<T, N, +1>, sm);
@@ -1307,79 +1271,6 @@ class EngineT final : public IEngine {
       launches_ = saved;
     });
     choose_plan();
-    tune_small();
-  }
-
-  // The single-cluster step of small grids (k_step_small) against the
-  // separate passes with the launch shapes just chosen: one fixed-dt step of
-  // the zero state each (it stays zero, and time does not advance), timed
-  // like the passes; R2D3C_SMALL=0/1 overrides.
-  void tune_small() {
-    small_on_ = false;
-    small_us_[0] = small_us_[1] = 0.f;
-    if (!small_ok_) return;
-    const int saved = launches_;
-    const std::vector<float> us = time_candidates(2, [&](size_t i) {
-      small_on_ = i == 1;
-      enqueue_step(false, false, 0, nullptr);
-    });
-    launches_ = saved;
-    small_us_[0] = us[0];
-    small_us_[1] = us[1];
-    small_on_ = us[1] < us[0];
-    if (const char* e = std::getenv("R2D3C_SMALL")) {
-      if (std::strcmp(e, "0") != 0 && std::strcmp(e, "1") != 0) throw Error(kEINVAL, "R2D3C_SMALL must be 0 or 1");
-      small_on_ = e[0] == '1';
-    }
-  }
-  // one step of a small grid as one cluster launch (k_step_small)
-  void launch_small(bool cfl_mode, bool add_time) {
-    dispatch_n(n_, [&](auto NC) {
-      constexpr int N = decltype(NC)::value;
-      if constexpr (SmallStep<T, N>::OK) {
-        using SS = SmallStep<T, N>;
-        SmallArgs<T> a;
-        a.ps = planes_[P_PS];
-        a.vz = planes_[P_VZ];
-        a.c1 = planes_[P_C1];
-        a.c2 = planes_[P_C2];
-        a.c3 = planes_[P_C3];
-        a.c4 = planes_[P_C4];
-        a.tf = tf_;
-        a.pb = pb_;
-        a.fp = planes_[P_FP];
-        a.fz = planes_[P_FZ];
-        a.tau5 = closure_on_ ? planes_[P_T5] : nullptr;
-        a.tau6 = closure_on_ ? planes_[P_T6] : nullptr;
-        a.tw = tw_;
-        a.twa = tw_a_;
-        a.scs = d_sc_;
-        a.scal = scal_base_;
-        a.enc = enc_base_;
-        a.cc = d_cfl_;
-        a.inv_n4 = (T)(1.0 / ((double)n_ * n_ * n_ * n_));
-        a.cfl_mode = cfl_mode ? 1 : 0;
-        a.add_time = add_time ? 1 : 0;
-        a.gd = gd_;
-        a.bs = batch();
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(small_ncl_, 1, 1);
-        cfg.blockDim = dim3(SS::THREADS, 1, 1);
-        cfg.dynamicSmemBytes = SS::SMEM;
-        cfg.stream = st_;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = small_ncl_;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        cuda_check(cudaLaunchKernelEx(&cfg, k_step_small<T, N>, a), "k_step_small");
-        post("k_step_small");
-      } else {
-        throw Error(kEINVAL, "small-grid step: unsupported n");
-      }
-    });
   }
 
   // The launch choices from the autotuner's timings.  Policy 0: the fastest
@@ -1480,7 +1371,7 @@ class EngineT final : public IEngine {
  public:
   std::string plan_report() const override {
     std::string r = "{\"policy\": " + std::to_string(policy_) + ", \"pass_a\": [";
-    char b[512];
+    char b[200];
     for (size_t i = 0; i < tune_a_.size(); ++i) {
       snprintf(b, sizeof b, "%s{\"radix\": %d, \"groups\": %d, \"field_chunks\": %d, \"us\": %.2f}",
                i ? ", " : "", tune_a_[i].radix, tune_a_[i].mode, tune_a_[i].grid, (double)tune_a_[i].us);
@@ -1511,12 +1402,8 @@ class EngineT final : public IEngine {
                  i ? ", " : "", tune_c_[i].grid, tune_c_[i].chunks, (double)tune_c_[i].us);
       r += b;
     }
-    snprintf(b, sizeof b,
-             "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d, \"chunks_c\": %d, \"small_step\": "
-             "{\"available\": %s, \"cluster\": %d, \"us_separate\": %.2f, \"us_cluster\": %.2f, \"chosen\": %s}}",
-             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_, fc_,
-             small_ok_ ? "true" : "false", small_ncl_, (double)small_us_[0], (double)small_us_[1],
-             small_on_ ? "true" : "false");
+    snprintf(b, sizeof b, "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d, \"chunks_c\": %d}",
+             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_, fc_);
     return r + b;
   }
 
@@ -1559,10 +1446,6 @@ class EngineT final : public IEngine {
   int policy_ = 0;      // plan policy (choose_plan)
   int ga_ = 0, fa_ = 1;  // pass A: groups per CTA (0: the config's G), field chunks (autotuned)
   int fc_ = 1;           // pass C: CTAs per column pair (1 or 2, autotuned)
-  bool small_ok_ = false;  // the single-cluster step can run (n <= 512, one run)
-  bool small_on_ = false;  // and the autotuner chose it
-  int small_ncl_ = 0;      // CTAs per cluster
-  float small_us_[2] = {0.f, 0.f};  // separate passes, single cluster (us per step)
   int gb_ = 0, gc_ = 0;  // passes B, C one CTA per row / column pair: groups per CTA (autotuned)
   struct TuneRec {
     int mode, grid;  // pass A: groups, field chunks; B, C: variant, CTAs or groups

@@ -301,17 +301,81 @@ template <typename T, int N, int EA = PassAE<T, N>::value>
 __global__ void __launch_bounds__(CfgAE<T, N, EA>::THREADS, (sizeof(T) == 4 && CfgAE<T, N, EA>::THREADS == 256) ? 2 : 1)
 k_passA(const cpx<T>* __restrict__ ps, const cpx<T>* __restrict__ vz, cpx<T>* __restrict__ tf,
         DevGrid gd, const tw_t<T>* __restrict__ tw, Batch bs) {
-#define R2D3C_VB_X blockIdx.x
-#define R2D3C_VB_Y blockIdx.y
-#define R2D3C_VB_Z blockIdx.z
-#define R2D3C_VB_NZ gridDim.z
-#define R2D3C_VB_GPC (blockDim.x / C::TPF)
-#include "r2d3c_pass_a.inc"
-#undef R2D3C_VB_X
-#undef R2D3C_VB_Y
-#undef R2D3C_VB_Z
-#undef R2D3C_VB_NZ
-#undef R2D3C_VB_GPC
+  constexpr int NT = PassNT<T, N>::value;
+  ps += blockIdx.y * bs.spec;
+  vz += blockIdx.y * bs.spec;
+  tf += blockIdx.y * bs.tf;
+  using C = CfgAE<T, N, EA>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  cpx<T>* sm = smbase_ + (size_t)g * NT * F::SMEM_ELEMS;
+  // groups per CTA and field chunks are launch-time choices (blockDim.x =
+  // groups * TPF, gridDim.z chunks of the six fields): small grids spread
+  // one column pair's fields over several CTAs; the arithmetic per field is
+  // the same whatever the split
+  const int kx0 = (blockIdx.x * (blockDim.x / C::TPF) + g) * NT;
+  const int fpc = 6 / gridDim.z, f0 = blockIdx.z * fpc;
+  const size_t plane = (size_t)gd.M * N;
+  int kyi[C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) kyi[q] = ky_of(lane + q * C::TPF, N);
+  // The source column (pair) is re-read for every field, from L2, rather
+  // than held in registers across the fields: the registers freed let FP32
+  // run two 256-thread CTAs per SM (and keep FP64 from spilling)
+  cpx<T> v[NT][C::E];
+  auto src_at = [&](const cpx<T>* sp, int t, int q) -> cpx<T> {
+    const int col = kx0 + t, ky = kyi[q];
+    const bool in = col < gd.M && (ky <= gd.L && -ky <= gd.L) && col * col + ky * ky <= gd.kmaxi;
+    return in ? sp[(size_t)col * N + lane + q * C::TPF] : czero<T>();
+  };
+#pragma unroll 1
+  for (int f = f0; f < f0 + fpc; ++f) {
+    const cpx<T>* sp = f < 4 ? ps : vz;  // psi for fields 0-3, vz for fields 4-5
+    {
+#pragma unroll
+      for (int t = 0; t < NT; ++t) {
+        const int col = kx0 + t;
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
+          const T k = (f & 1) ? (T)kyi[q] : (T)col;
+          cpx<T> x = src_at(sp, t, q);
+          if (f == 2 || f == 3) {
+            const T m = -(T)(col * col + kyi[q] * kyi[q]);  // laplak2: -ka2*a
+            x = mkc<T>(m * x.x, m * x.y);
+          }
+          v[t][q] = mkc<T>(-k * x.y, k * x.x);
+        }
+      }
+      F::template run<+1>(v, lane, sm, tw);
+      cpx<T>* dst = tf + (size_t)f * plane;
+      if constexpr (NT == 2) {
+        // lanes (2p, 2p+1) hold rows y = 2p, 2p+1 of columns kx0, kx0+1: swap
+        // one value so each lane writes one column's row pair (16 bytes)
+        const bool odd = lane & 1;
+        const int kx = kx0 + (odd ? 1 : 0);
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          const cpx<T> give = odd ? v[0][q] : v[1][q];
+          cpx<T> got;
+          got.x = __shfl_xor_sync(0xffffffffu, give.x, 1);
+          got.y = __shfl_xor_sync(0xffffffffu, give.y, 1);
+          const int y = (lane + q * C::TPF) & ~1;
+          if (kx < gd.M) {
+            const cpx<T> lo = odd ? got : v[0][q];
+            const cpx<T> hi = odd ? v[1][q] : got;
+            *reinterpret_cast<float4*>(dst + mix_idx<N, 2>(kx, y, gd.M)) = make_float4(lo.x, lo.y, hi.x, hi.y);
+          }
+        }
+      } else {
+        if (kx0 < gd.M) {
+#pragma unroll
+          for (int q = 0; q < C::E; ++q) dst[(size_t)kx0 * N + lane + q * C::TPF] = v[0][q];
+        }
+      }
+    }
+  }
 }
 
 // NR consecutive rows y0.. of a mixed plane at column kx: one 16-byte load
@@ -402,17 +466,145 @@ template <typename T, int N, bool CFL>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
         const tw_t<T>* __restrict__ tw, unsigned long long* __restrict__ cfl_enc, Batch bs) {
-#define R2D3C_VB_X blockIdx.x
-#define R2D3C_VB_Y blockIdx.y
-#define R2D3C_VB_Z blockIdx.z
-#define R2D3C_VB_NZ gridDim.z
-#define R2D3C_VB_GPC (blockDim.x / C::TPF)
-#include "r2d3c_pass_b.inc"
-#undef R2D3C_VB_X
-#undef R2D3C_VB_Y
-#undef R2D3C_VB_Z
-#undef R2D3C_VB_NZ
-#undef R2D3C_VB_GPC
+  constexpr int NR = PassNT<T, N>::value;
+  using PS = PassSmem<T, N>;
+  constexpr bool HOLD = PS::HOLD;
+  tf += blockIdx.y * bs.tf;
+  pb += blockIdx.y * bs.pb;
+  cfl_enc += blockIdx.y * kScalStride;
+  using C = Cfg<T, N, NR>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
+  cpx<T>* hold = sm + NR * F::SMEM_ELEMS;  // z1 store (HOLD)
+  int rg = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
+  const bool ok = rg < N / NR;
+  if (!ok) rg = 0;  // surplus groups recompute rows 0.. and store nothing
+  const int y0 = rg * NR;
+  const int M = gd.M;
+  const size_t plane = (size_t)M * N;
+  cpx<T> v[NR][C::E];
+  if constexpr (RolledB<T, N>::OK) {
+    T* P1 = reinterpret_cast<T*>(smbase_ + (size_t)(blockDim.x / C::TPF) * PS::GROUP_ELEMS) + (size_t)g * N;
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+      if (f < 3) {
+        const cpx<T>* pa = tf + (size_t)(2 * f) * plane;
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          cpx<T> z[1];
+          packed_pair<T, N, 1>(pa, pa + plane, lane + q * C::TPF, y0, M, z);
+          v[0][q] = z[0];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) v[0][q].y = -v[0][q].y;
+      }
+      F::template run<+1>(v, lane, sm, tw);
+      // each thread reads back only the positions it wrote: no barrier needed
+      if (f == 0) {
+        if constexpr (CFL) cfl_max_sq<T, 1, C::E>(v, cfl_enc);
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) hold[lane + q * C::TPF] = v[0][q];
+      } else if (f == 1) {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          const cpx<T> a = hold[lane + q * C::TPF];
+          P1[lane + q * C::TPF] = (a.x * v[0][q].y - a.y * v[0][q].x) * inv_n4;
+        }
+      } else if (f == 2) {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          const cpx<T> a = hold[lane + q * C::TPF];
+          v[0][q] = mkc<T>(P1[lane + q * C::TPF], (a.x * v[0][q].y - a.y * v[0][q].x) * inv_n4);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) v[0][q].y = -v[0][q].y;
+      }
+    }
+  } else {
+  cpx<T> z1r[HOLD ? 1 : NR][C::E];
+  T p1[NR][C::E];
+  // pair (d_x psi, d_y psi)
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    cpx<T> z[NR];
+    packed_pair<T, N, NR>(tf, tf + plane, lane + q * C::TPF, y0, M, z);
+#pragma unroll
+    for (int t = 0; t < NR; ++t) v[t][q] = z[t];
+  }
+  F::template run<+1>(v, lane, sm, tw);
+  if constexpr (CFL) cfl_max_sq<T, NR, C::E>(v, cfl_enc);
+  // each thread reads back only the positions it wrote: no barrier needed
+  auto z1 = [&](int t, int q) -> cpx<T> {
+    if constexpr (HOLD) return hold[t * N + lane + q * C::TPF];
+    else return z1r[t][q];
+  };
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      if constexpr (HOLD) hold[t * N + lane + q * C::TPF] = v[t][q];
+      else z1r[t][q] = v[t][q];
+    }
+  // pair (d_x(-k^2 psi), d_y(-k^2 psi)) -> [psi, -k^2 psi]
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    cpx<T> z[NR];
+    packed_pair<T, N, NR>(tf + 2 * plane, tf + 3 * plane, lane + q * C::TPF, y0, M, z);
+#pragma unroll
+    for (int t = 0; t < NR; ++t) v[t][q] = z[t];
+  }
+  F::template run<+1>(v, lane, sm, tw);
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      const cpx<T> a = z1(t, q);
+      p1[t][q] = (a.x * v[t][q].y - a.y * v[t][q].x) * inv_n4;
+    }
+  // pair (d_x vz, d_y vz) -> [psi, vz]
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    cpx<T> z[NR];
+    packed_pair<T, N, NR>(tf + 4 * plane, tf + 5 * plane, lane + q * C::TPF, y0, M, z);
+#pragma unroll
+    for (int t = 0; t < NR; ++t) v[t][q] = z[t];
+  }
+  F::template run<+1>(v, lane, sm, tw);
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      const cpx<T> a = z1(t, q);
+      v[t][q] = mkc<T>(p1[t][q], (a.x * v[t][q].y - a.y * v[t][q].x) * inv_n4);
+    }
+  // forward x-FFT of both real products at once
+  F::template run<-1>(v, lane, sm, tw);
+  }
+  F::to_smem(v, lane, sm);
+  fft_sync<C::TPF>();
+  const size_t oplane = (size_t)gd.nh * N;
+  const T h = (T)0.5;
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) {
+    const int k = lane + q * C::TPF;
+    if (ok && k < kxo) {
+      cpx<T> o1[NR], o2[NR];
+#pragma unroll
+      for (int t = 0; t < NR; ++t) {
+        const cpx<T> w = F::from_smem(t, k, sm);
+        const cpx<T> u = F::from_smem(t, (N - k) & (N - 1), sm);
+        o1[t] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
+        o2[t] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+      }
+      const size_t off = mix_idx<N, NR>(k, y0, gd.nh);
+      store_rows<T, NR>(pb, off, o1);
+      store_rows<T, NR>(pb + oplane, off, o2);
+    }
+  }
 }
 
 // --------------------------------------------------------------------------
@@ -839,17 +1031,178 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         const StepCoef* __restrict__ scs, const double* __restrict__ scal, int o,
         const tw_t<T>* __restrict__ tw, Batch bs, const cpx<T>* __restrict__ tau5,
         const cpx<T>* __restrict__ tau6) {
-#define R2D3C_VB_X blockIdx.x
-#define R2D3C_VB_Y blockIdx.y
-#define R2D3C_VB_Z blockIdx.z
-#define R2D3C_VB_NZ gridDim.z
-#define R2D3C_VB_GPC (blockDim.x / C::TPF)
-#include "r2d3c_pass_c.inc"
-#undef R2D3C_VB_X
-#undef R2D3C_VB_Y
-#undef R2D3C_VB_Z
-#undef R2D3C_VB_NZ
-#undef R2D3C_VB_GPC
+  constexpr int NT = PassNT<T, N>::value;
+  using PS = PassSmem<T, N>;
+  constexpr bool HOLD = PS::HOLD;
+  const size_t rs = blockIdx.y * bs.spec;
+  pb += blockIdx.y * bs.pb;
+  c1in += rs;
+  c2in += rs;
+  ps += rs;
+  vz += rs;
+  fp += rs;
+  fz += rs;
+  c1out += rs;
+  c2out += rs;
+  using C = Cfg<T, N, NT>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane0 = threadIdx.x % C::TPF;
+  cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
+  cpx<T>* hold = sm + NT * F::SMEM_ELEMS;  // transformed [psi,-k^2 psi] columns (HOLD)
+  const int kx0 = (blockIdx.x * (blockDim.x / C::TPF) + g) * NT;  // groups per CTA: a launch-time choice
+  const size_t oplane = (size_t)gd.nh * N;
+  // The RK update at the end reads six spectral planes (eight with the
+  // closure tendencies) on this group's columns; they are prefetched into L2
+  // now, while the transforms run, so that those reads do not wait for DRAM.
+  if (lane0 < 8) {
+    const int lane = lane0;
+    const cpx<T>* src = lane == 0 ? c1in : lane == 1 ? c2in : lane == 2 ? ps : lane == 3 ? vz
+                      : lane == 4 ? fp : lane == 5 ? fz : lane == 6 ? tau5 : tau6;
+    // with two chunks each CTA needs half of them: z = 0 the C1 update's
+    // (c2in, ps, fp, tau5), z = 1 the C2 update's (c1in, vz, fz, tau6)
+    const int user = lane < 2 ? 1 - lane : (lane & 1);  // the chunk that reads src
+    const bool need = gridDim.z == 1 || !(sizeof(T) == 4 && HOLD) || (int)blockIdx.z == user;
+    const int ncol = min(NT, gd.M - kx0);
+    if (src && need && ncol > 0) prefetch_columns_l2<T>(src + (size_t)kx0 * N, ncol, N, gd.L);
+  }
+  cpx<T> v[NT][C::E];
+  cpx<T> c5r[HOLD ? 1 : NT][C::E];
+  // gridDim.z = 2 splits a column pair's work over two CTAs (FP32 grids with
+  // the held c5): z = 0 transforms [psi,-k^2 psi] and updates C1, z = 1
+  // transforms [psi, vz] and updates C2; the arithmetic per element is the
+  // same as with one CTA (the launch autotuner chooses)
+  const int chunk = (HOLD && sizeof(T) == 4 && gridDim.z > 1) ? (int)blockIdx.z : -1;
+#pragma unroll 1
+  for (int pl = 0; pl < 2; ++pl) {
+    if (chunk >= 0 && pl != chunk) continue;
+    // the loop-invariant addresses of the transform are recomputed per
+    // iteration from an opaque copy of the lane index instead of being
+    // hoisted out of the loop and held in registers across it
+    const int lane = opaque(lane0);
+    const cpx<T>* src = pb + pl * oplane;
+    if constexpr (NT == 2) {
+      // lane pair (2p, 2p+1): the even lane loads column kx0's rows (2p, 2p+1),
+      // the odd lane column kx0+1's; one swap gives each lane its own row of
+      // both columns
+      const bool odd = lane & 1;
+      const int kx = kx0 + (odd ? 1 : 0);
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) {
+        const int y = (lane + q * C::TPF) & ~1;
+        const float4 w = __ldg(reinterpret_cast<const float4*>(src + mix_idx<N, 2>(kx, y, gd.nh)));
+        const float gx = odd ? w.x : w.z, gy = odd ? w.y : w.w;  // value the partner needs
+        const float rx = __shfl_xor_sync(0xffffffffu, gx, 1);
+        const float ry = __shfl_xor_sync(0xffffffffu, gy, 1);
+        if (odd) {
+          v[0][q] = mkc<T>(rx, ry);
+          v[1][q] = mkc<T>(w.z, w.w);
+        } else {
+          v[0][q] = mkc<T>(w.x, w.y);
+          v[1][q] = mkc<T>(rx, ry);
+        }
+      }
+    } else {
+      const cpx<T>* s5 = src + (size_t)(kx0 < gd.M ? kx0 : 0) * N;
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) v[0][q] = s5[lane + q * C::TPF];
+    }
+    F::template run<-1>(v, lane, sm, tw);
+    if (pl == 0) {
+#pragma unroll
+      for (int t = 0; t < NT; ++t)
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          if constexpr (HOLD) hold[t * N + lane + q * C::TPF] = v[t][q];
+          else c5r[t][q] = v[t][q];
+        }
+    }
+  }
+  const int lane = lane0;
+  // v holds the transformed [psi, vz] columns (c6).  The coefficients are
+  // read only now, not held in registers across the transforms.
+  const StepCoef sc = scs[blockIdx.y];
+  const T tmp1 = (T)(scal[blockIdx.y * kScalStride] / (double)o);  // :581
+  if constexpr (HOLD && sizeof(T) == 4) {
+    passC_update_pairs<T, N, NT, C::E, C::TPF>(sm, hold, v, lane, kx0, c1in, c2in, ps, vz, fp, fz, c1out, c2out, gd,
+                                                sc, tmp1, tau5, tau6, chunk);
+  } else if constexpr (HOLD) {
+    // c6 joins c5 in shared memory (the transform buffer is free after the
+    // last transform; each thread reads back only what it wrote), and the
+    // update runs over this thread's elements in batches of RB: all loads of
+    // a batch, then its arithmetic and stores.
+    cpx<T>* c6s = sm;
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) c6s[t * N + lane + q * C::TPF] = v[t][q];
+    constexpr int NE = NT * C::E, RB = 2;
+    static_assert(NE % RB == 0, "whole batches");
+#pragma unroll 1
+    for (int e0 = 0; e0 < NE; e0 += RB) {
+      RkIn<T> in[RB];
+      cpx<T> ta[RB], tb[RB];
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const int t = (e0 + b) / C::E, q = (e0 + b) % C::E;
+        const int col = kx0 + t, j = lane + q * C::TPF, ky = ky_of(j, N), k2 = col * col + ky * ky;
+        if (col < gd.M && k2 <= gd.kmaxi && k2 >= 1) {
+          const size_t idx = (size_t)col * N + j;
+          rk_load<T>(in[b], idx, c1in, c2in, ps, vz, fp, fz);
+          if (tau5) {
+            ta[b] = tau5[idx];
+            tb[b] = tau6[idx];
+          }
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const int t = (e0 + b) / C::E, q = (e0 + b) % C::E;
+        const int col = kx0 + t, j = lane + q * C::TPF, ky = ky_of(j, N), k2 = col * col + ky * ky;
+        if (col >= gd.M || ky > gd.L || -ky > gd.L) continue;
+        cpx<T> n1 = czero<T>(), n2 = czero<T>();
+        if (k2 <= gd.kmaxi && k2 >= 1) {  // ka2 <= kmax .and. ka2 > tiny (:580)
+          cpx<T> c5 = hold[t * N + j], c6 = c6s[t * N + j];
+          if (tau5) {  // learned subgrid tendencies of the two brackets
+            c5 = mkc<T>(c5.x + ta[b].x, c5.y + ta[b].y);
+            c6 = mkc<T>(c6.x + tb[b].x, c6.y + tb[b].y);
+          }
+          rk_apply<T>(in[b], c5, c6, ky, k2, sc, tmp1, n1, n2);
+        }
+        const size_t idx = (size_t)col * N + j;
+        c1out[idx] = n1;
+        c2out[idx] = n2;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int col = kx0 + t;
+      if (col >= gd.M) continue;
+#pragma unroll
+      for (int q = 0; q < C::E; ++q) {
+        const int j = lane + q * C::TPF;
+        const int ky = ky_of(j, N);
+        if (ky > gd.L || -ky > gd.L) continue;
+        const int k2 = col * col + ky * ky;
+        cpx<T> n1 = czero<T>(), n2 = czero<T>();
+        const size_t idx = (size_t)col * N + j;
+        if (k2 <= gd.kmaxi && k2 >= 1) {
+          cpx<T> c5 = c5r[t][q], c6 = v[t][q];
+          if (tau5) {
+            const cpx<T> a = tau5[idx], b = tau6[idx];
+            c5 = mkc<T>(c5.x + a.x, c5.y + a.y);
+            c6 = mkc<T>(c6.x + b.x, c6.y + b.y);
+          }
+          RkIn<T> in;
+          rk_load<T>(in, idx, c1in, c2in, ps, vz, fp, fz);
+          rk_apply<T>(in, c5, c6, ky, k2, sc, tmp1, n1, n2);
+        }
+        c1out[idx] = n1;
+        c2out[idx] = n2;
+      }
+    }
+  }
 }
 
 // --------------------------------------------------------------------------
