@@ -1018,6 +1018,14 @@ class EngineT final : public IEngine {
           post("k_passB_pipe");
         }
       }
+      if constexpr (SplitB<T, N>::OK) {
+        if (passb_mode_ == 2) {  // three CTA groups per row pair (small grids)
+          persistent = true;
+          k_passB_split<T, N, CFL><<<dim3(N / NR, nb), SplitB<T, N>::THREADS, SplitB<T, N>::SMEM, st_>>>(
+              tf, pb, kxo, gd_, inv4, tw_, enc_base_, batch());
+          post("k_passB_split");
+        }
+      }
       if (!persistent) {  // one CTA (group) per row pair; the only form below n = 2048
         auto k = k_passB<T, N, CFL>;
         const int g = gb_ ? gb_ : C::G;  // groups per CTA: autotuned
@@ -1082,6 +1090,10 @@ class EngineT final : public IEngine {
       if constexpr (kAltRadixA<T, N>) set_smem_attr(k_passA<T, N, Cfg<T, N>::E>, CfgAE<T, N, Cfg<T, N>::E>::SMEM);
       set_smem_attr(k_passB<T, N, true>, RolledB<T, N>::SMEM);
       set_smem_attr(k_passB<T, N, false>, RolledB<T, N>::SMEM);
+      if constexpr (SplitB<T, N>::OK) {
+        set_smem_attr(k_passB_split<T, N, true>, SplitB<T, N>::SMEM);
+        set_smem_attr(k_passB_split<T, N, false>, SplitB<T, N>::SMEM);
+      }
       set_smem_attr(k_passC<T, N>, smh);
       if constexpr (kPipeC<T, N>) {
         set_smem_attr(k_passC_pipe<N>, PipeC<N>::SMEM);
@@ -1221,9 +1233,10 @@ class EngineT final : public IEngine {
           cands.push_back({1, pipeb_ctas_});
           if (pipeb_ctas_ >= 2 * sms) cands.push_back({1, pipeb_ctas_ / 2});
         }
+        if constexpr (SplitB<T, N>::OK) cands.push_back({2, 1});
         const std::vector<float> us = time_candidates(cands.size(), [&](size_t i) {
           passb_mode_ = cands[i].first;
-          pipeb_grid_ = cands[i].first ? cands[i].second : 0;
+          pipeb_grid_ = cands[i].first == 1 ? cands[i].second : 0;
           gb_ = cands[i].first ? GB : cands[i].second;
           launch_passB<false>(gd_.M, tf_, pb_, nb_);
         });
@@ -1333,7 +1346,7 @@ class EngineT final : public IEngine {
       fa_ = forced[1] >= 0 ? forced[1] : tune_a_[ka].grid;
       auto pick_bc = [&](const std::vector<TuneRec>& t, const char* env, const char* pair_name, int forced_g,
                          int& mode, int& grid, int& groups) {
-        auto ok = [&](const TuneRec& r) { return pol == 0 || r.mode == 1 || r.grid == GB; };
+        auto ok = [&](const TuneRec& r) { return pol == 0 || r.mode == 1 || (r.mode == 0 && r.grid == GB); };
         const size_t pick0 = argmin(t, [&](const TuneRec& r) { return r.mode == 0 && ok(r); });
         size_t pick = argmin(t, ok);
         // env=<pair_name>|persistent overrides the measured choice
@@ -1341,6 +1354,12 @@ class EngineT final : public IEngine {
         if (const char* force = std::getenv(env)) {
           if (std::strcmp(force, pair_name) == 0) {
             pick = pick0;
+          } else if (std::strcmp(force, "split") == 0) {
+            // three groups per row pair, where it exists (pass B of small grids)
+            size_t k = t.size();
+            for (size_t i = 0; i < t.size(); ++i)
+              if (t[i].mode == 2) k = i;
+            pick = k < t.size() ? k : pick0;
           } else if (std::strcmp(force, "persistent") == 0) {
             // the first persistent candidate: all resident CTAs
             size_t k = t.size();
@@ -1348,11 +1367,11 @@ class EngineT final : public IEngine {
               if (t[i].mode == 1) k = i;
             pick = k < t.size() ? k : pick0;
           } else {
-            throw Error(kEINVAL, std::string(env) + " must be " + pair_name + " or persistent");
+            throw Error(kEINVAL, std::string(env) + " must be " + pair_name + ", persistent or split");
           }
         }
         mode = t[pick].mode;
-        grid = mode ? t[pick].grid : 0;
+        grid = mode == 1 ? t[pick].grid : 0;
         groups = forced_g >= 0 ? (forced_g ? forced_g : GB) : t[pick0].grid;
         return pick0;
       };
@@ -1381,7 +1400,9 @@ class EngineT final : public IEngine {
              radix_a_, ga_, fa_);
     r += b;
     for (size_t i = 0; i < tune_.size(); ++i) {
-      if (tune_[i].mode)
+      if (tune_[i].mode == 2)
+        snprintf(b, sizeof b, "%s{\"variant\": \"split\", \"us\": %.2f}", i ? ", " : "", (double)tune_[i].us);
+      else if (tune_[i].mode)
         snprintf(b, sizeof b, "%s{\"variant\": \"persistent\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
                  tune_[i].grid, (double)tune_[i].us);
       else
@@ -1390,7 +1411,8 @@ class EngineT final : public IEngine {
       r += b;
     }
     snprintf(b, sizeof b, "], \"chosen\": \"%s\", \"ctas\": %d, \"groups_b\": %d",
-             passb_mode_ ? "persistent" : "per_row_pair", passb_mode_ ? pipeb_grid_ : 0, gb_);
+             passb_mode_ == 2 ? "split" : passb_mode_ ? "persistent" : "per_row_pair", passb_mode_ == 1 ? pipeb_grid_ : 0,
+             gb_);
     r += b;
     r += ", \"pass_c\": [";
     for (size_t i = 0; i < tune_c_.size(); ++i) {

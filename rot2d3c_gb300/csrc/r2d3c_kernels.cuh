@@ -608,6 +608,109 @@ k_passB(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid
 }
 
 // --------------------------------------------------------------------------
+// Pass B for small grids, the three inverse transforms of a row pair side by
+// side: a CTA of three groups per row pair, group j transforming the packed
+// pair (planes 2j, 2j+1), so the serial chain is one inverse and one forward
+// transform instead of four transforms (small grids are bound by that chain,
+// not by throughput).  The three results meet in shared memory; every group
+// then forms the two brackets and runs the forward transform (the same
+// values: keeping all groups in step keeps every barrier uniform), and
+// group 0 stores.  Same arithmetic, in the same order, as k_passB:
+// bit-identical (the launch autotuner chooses).
+// --------------------------------------------------------------------------
+template <typename T, int N>
+struct SplitB {
+  static constexpr int NR = PassNT<T, N>::value;
+  using C = Cfg<T, N, NR>;
+  using F = typename C::FFT;
+  static constexpr int TPF = C::TPF;
+  static constexpr int THREADS = 3 * TPF;
+  static constexpr bool OK = THREADS <= 384;
+  static constexpr size_t SMEM = 3 * F::SMEM_BYTES + (size_t)3 * NR * N * sizeof(cpx<T>);
+};
+
+template <typename T, int N, bool CFL>
+__global__ void __launch_bounds__(SplitB<T, N>::THREADS)
+k_passB_split(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, DevGrid gd, T inv_n4,
+              const tw_t<T>* __restrict__ tw, unsigned long long* __restrict__ cfl_enc, Batch bs) {
+  using SB = SplitB<T, N>;
+  constexpr int NR = SB::NR, E = SB::C::E, TPF = SB::TPF;
+  using F = typename SB::F;
+  tf += blockIdx.y * bs.tf;
+  pb += blockIdx.y * bs.pb;
+  cfl_enc += blockIdx.y * kScalStride;
+  R2D3C_SMEM_DECL
+  const int j = threadIdx.x / TPF, lane = threadIdx.x % TPF;
+  cpx<T>* sm = reinterpret_cast<cpx<T>*>(smraw_ + (size_t)j * F::SMEM_BYTES);
+  cpx<T>* res = reinterpret_cast<cpx<T>*>(smraw_ + 3 * F::SMEM_BYTES);  // [pair j][row t][x]
+  const int y0 = blockIdx.x * NR;
+  const int M = gd.M;
+  const size_t plane = (size_t)M * N;
+  cpx<T> v[NR][E];
+#pragma unroll
+  for (int q = 0; q < E; ++q) {
+    cpx<T> z[NR];
+    packed_pair<T, N, NR>(tf + (size_t)(2 * j) * plane, tf + (size_t)(2 * j + 1) * plane, lane + q * TPF, y0, M,
+                          z);
+#pragma unroll
+    for (int t = 0; t < NR; ++t) v[t][q] = z[t];
+  }
+  F::template run<+1>(v, lane, sm, tw);
+  if constexpr (CFL) {  // CFL maximum of |grad psi|^2 from z1 (cfl_max_sq; every lane joins the shuffles)
+    T m = (T)0;
+    if (j == 0) {
+#pragma unroll
+      for (int t = 0; t < NR; ++t)
+#pragma unroll
+        for (int q = 0; q < E; ++q) m = max(m, v[t][q].x * v[t][q].x + v[t][q].y * v[t][q].y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(cfl_enc, enc_ordered((double)m));
+  }
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < E; ++q) res[((size_t)j * NR + t) * N + lane + q * TPF] = v[t][q];
+  __syncthreads();
+  // [psi, -k^2 psi] and [psi, vz] from z1 (pair 0) with z2, z3 (pairs 1, 2)
+#pragma unroll
+  for (int t = 0; t < NR; ++t)
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int x = lane + q * TPF;
+      const cpx<T> a = res[(size_t)t * N + x];
+      const cpx<T> b = res[((size_t)NR + t) * N + x];
+      const cpx<T> c = res[((size_t)2 * NR + t) * N + x];
+      const T p1 = (a.x * b.y - a.y * b.x) * inv_n4;
+      v[t][q] = mkc<T>(p1, (a.x * c.y - a.y * c.x) * inv_n4);
+    }
+  F::template run<-1>(v, lane, sm, tw);
+  F::to_smem(v, lane, sm);
+  fft_sync<TPF>();
+  if (j != 0) return;  // (no barrier follows)
+  const size_t oplane = (size_t)gd.nh * N;
+  const T h = (T)0.5;
+#pragma unroll
+  for (int q = 0; q < E; ++q) {
+    const int k = lane + q * TPF;
+    if (k < kxo) {
+      cpx<T> o1[NR], o2[NR];
+#pragma unroll
+      for (int t = 0; t < NR; ++t) {
+        const cpx<T> w = F::from_smem(t, k, sm);
+        const cpx<T> u = F::from_smem(t, (N - k) & (N - 1), sm);
+        o1[t] = mkc<T>((w.x + u.x) * h, (w.y - u.y) * h);
+        o2[t] = mkc<T>((w.y + u.y) * h, (u.x - w.x) * h);
+      }
+      const size_t off = mix_idx<N, NR>(k, y0, gd.nh);
+      store_rows<T, NR>(pb, off, o1);
+      store_rows<T, NR>(pb + oplane, off, o2);
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
 // Pass B, FP32 pair-tiled grids (n = 512 .. 4096), one row pair per CTA at a
 // time: persistent CTAs that stage each row pair's mixed-plane inputs in
 // shared memory with asynchronous copies (cp.async, 16 bytes per thread and

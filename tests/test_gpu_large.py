@@ -92,15 +92,17 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
     cp, ps, vz, fp, fz = _case(n, 11)
     c = gpu.Context(cp, 1)
     rep = c.plan_report()
-    assert {r["variant"] for r in rep["pass_b"]} == {"per_row_pair", "persistent"}
+    variants_b = {r["variant"] for r in rep["pass_b"]}
+    assert variants_b == ({"per_row_pair", "persistent", "split"} if n <= 1024 else {"per_row_pair", "persistent"})
     assert rep["pass_a"] and all(r["us"] > 0 for r in rep["pass_a"])
-    assert all(r["us"] > 0 for r in rep["pass_b"]) and rep["chosen"] in ("per_row_pair", "persistent")
+    assert all(r["us"] > 0 for r in rep["pass_b"]) and rep["chosen"] in variants_b
     assert {r["variant"] for r in rep["pass_c"]} == {"per_column_pair", "persistent"}
     assert all(r["us"] > 0 for r in rep["pass_c"]) and rep["chosen_c"] in ("per_column_pair", "persistent")
     c.destroy()
     out = []
     for mb, mc, groups in (("per_row_pair", "per_column_pair", None), ("persistent", "persistent", None),
-                           ("persistent", "per_column_pair", None), ("persistent", "per_column_pair", "0,1,0,0,2")):
+                           ("persistent", "per_column_pair", None), ("persistent", "per_column_pair", "0,1,0,0,2"),
+                           ("split" if n <= 1024 else "persistent", "persistent", None)):
         monkeypatch.setenv("R2D3C_PASSB", mb)
         monkeypatch.setenv("R2D3C_PASSC", mc)
         if groups:
@@ -119,7 +121,8 @@ def test_autotuned_pass_b_variants_are_bit_identical(gpu, monkeypatch, n):
         for u, v in zip(out[0], o):
             np.testing.assert_array_equal(u, v)
     small = gpu.Context(params(64, iflow=0)[1], 1).plan_report()
-    assert {r["variant"] for r in small["pass_b"]} == {"per_row_pair"} and small["chosen"] == "per_row_pair"
+    assert {r["variant"] for r in small["pass_b"]} == {"per_row_pair", "split"} and small["chosen"] in (
+        "per_row_pair", "split")
     assert {r["variant"] for r in small["pass_c"]} == {"per_column_pair"} and small["chosen_c"] == "per_column_pair"
 
 
@@ -129,12 +132,12 @@ def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
     shapes only: every forced choice steps to the same bits as the tuned one."""
     cp, ps, vz, fp, fz = _case(n, 5)
     out, reps = [], []
-    for forced in (None, "1,6,1,1", "0,1,0,0", "2,3,1,2", "0,1,0,1,2", "1,2,1,2,2"):
+    for forced in (None, "1,6,1,1", "0,1,0,0", "2,3,1,2", "0,1,0,1,2", "1,2,1,2,2", "split"):
         if forced is None:
             monkeypatch.delenv("R2D3C_GROUPS", raising=False)
-        else:
+        elif forced != "split":
             monkeypatch.setenv("R2D3C_GROUPS", forced)
-        monkeypatch.setenv("R2D3C_PASSB", "per_row_pair")
+        monkeypatch.setenv("R2D3C_PASSB", "split" if forced == "split" else "per_row_pair")
         monkeypatch.setenv("R2D3C_PASSC", "per_column_pair")
         c = gpu.Context(cp, prec)
         reps.append(c.plan_report())
@@ -148,6 +151,7 @@ def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
     assert reps[3]["field_chunks_a"] == 3
     # pass C's C1 and C2 updates split over two CTAs per column pair (FP32)
     assert reps[4]["chunks_c"] == (2 if prec == 1 else 1) and reps[5]["groups_c"] == 2
+    assert reps[6]["chosen"] == "split"
     for o in out[1:]:
         for u, v in zip(out[0], o):
             np.testing.assert_array_equal(u, v)
