@@ -121,7 +121,8 @@ def plan_summary_dict(r):
     return {"pass_a": {"radix": r.get("radix_a"), "groups": r["groups_a"], "field_chunks": r["field_chunks_a"]},
             "pass_b": r["chosen"] if r["chosen"] in ("persistent", "split") else f"per_row_pair x{r['groups_b']}",
             "pass_c": r["chosen_c"] if r["chosen_c"] == "persistent"
-            else f"per_column_pair x{r['groups_c']}" + (f" ({r['chunks_c']} CTAs per pair)" if r.get("chunks_c", 1) > 1 else "")}
+            else f"per_column_pair x{r['groups_c']}" + (f" ({r['chunks_c']} CTAs per pair)" if r.get("chunks_c", 1) > 1 else "")
+            + (f" (teams of {r['team_c']})" if r.get("team_c", 1) > 1 else "")}
 
 
 def workload_inputs(n):

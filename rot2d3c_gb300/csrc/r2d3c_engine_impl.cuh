@@ -1061,11 +1061,14 @@ class EngineT final : public IEngine {
         auto k = k_passC<T, N>;
         const int groups = (gd_.M + NT - 1) / NT;
         const int g = gc_ ? gc_ : C::G;  // groups per CTA: autotuned
-        // the C1 and C2 updates of a column pair in one CTA or two (autotuned)
-        const dim3 grid((groups + g - 1) / g, nb, kChunkC<T, N> ? fc_ : 1);
+        // the C1 and C2 updates of a column pair in one CTA or two, and
+        // teams of wc_ groups per column pair (autotuned)
+        const int w = kChunkC<T, N> ? wc_ : 1;
+        const int teams = std::max(1, g / w);
+        const dim3 grid((groups + teams - 1) / teams, nb, kChunkC<T, N> ? fc_ : 1);
         k<<<grid, C::TPF * g, g * PassSmem<T, N>::GROUP_ELEMS * sizeof(cpx<T>), st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ],
                                                            pbase_[P_FP], pbase_[P_FZ], c1out, c2out, gd_, d_sc_,
-                                                           scal_base_, o, tw_, batch(), t5, t6);
+                                                           scal_base_, o, tw_, batch(), t5, t6, w);
         post("k_passC");
       }
     });
@@ -1174,17 +1177,20 @@ class EngineT final : public IEngine {
   }
   // R2D3C_GROUPS="ga,fa,gb,gc" fixes the groups per CTA of passes A, B, C
   // and pass A's field chunks (0 for a group count: the config's G)
-  static void forced_groups(int G_A, int G_B, int G_C, int out[5]) {
+  static void forced_groups(int G_A, int G_B, int G_C, int out[6]) {
     out[0] = out[2] = out[3] = -1;
     out[1] = -1;
-    out[4] = -1;
+    out[4] = out[5] = -1;
     const char* e = std::getenv("R2D3C_GROUPS");
     if (!e) return;
-    int v[5] = {0, 0, 0, 0, -1};
-    const int got = std::sscanf(e, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]);
-    if (got != 4 && got != 5) throw Error(kEINVAL, "R2D3C_GROUPS must be ga,fa,gb,gc[,cc]");
-    if (got == 5 && v[4] != 1 && v[4] != 2) throw Error(kEINVAL, "R2D3C_GROUPS: pass C chunks must be 1 or 2");
-    out[4] = got == 5 ? v[4] : -1;
+    int v[6] = {0, 0, 0, 0, -1, -1};
+    const int got = std::sscanf(e, "%d,%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5]);
+    if (got < 4) throw Error(kEINVAL, "R2D3C_GROUPS must be ga,fa,gb,gc[,cc[,cw]]");
+    if (got >= 5 && v[4] != 1 && v[4] != 2) throw Error(kEINVAL, "R2D3C_GROUPS: pass C chunks must be 1 or 2");
+    if (got == 6 && v[5] != 1 && v[5] != 2 && v[5] != 4)
+      throw Error(kEINVAL, "R2D3C_GROUPS: pass C team must be 1, 2 or 4 groups");
+    out[4] = got >= 5 ? v[4] : -1;
+    out[5] = got == 6 ? v[5] : -1;
     auto group_ok = [](int g, int G) { return g == 0 || (g >= 1 && g <= G && (g & (g - 1)) == 0); };
     if (!group_ok(v[0], G_A) || !group_ok(v[2], G_B) || !group_ok(v[3], G_C) ||
         !(v[1] == 1 || v[1] == 2 || v[1] == 3 || v[1] == 6))
@@ -1250,16 +1256,21 @@ class EngineT final : public IEngine {
         cuda_check(cudaMemsetAsync(d_sc_, 0, sizeof(StepCoef) * nb_, st_), "memset");
         coefs_valid_ = false;
         struct CandC {
-          int mode, grid, chunks;
+          int mode, grid, chunks, wide;
         };
         std::vector<CandC> cands;
         for (int g = GB; g >= 1; g /= 2) {
-          cands.push_back({0, g, 1});
-          if constexpr (kChunkC<T, N>) cands.push_back({0, g, 2});
+          cands.push_back({0, g, 1, 1});
+          if constexpr (kChunkC<T, N>) {
+            cands.push_back({0, g, 2, 1});
+            // teams of 2 or 4 groups per column pair share its update
+            for (int w : {2, 4})
+              if (w <= g) cands.push_back({0, g, 2, w});
+          }
         }
         if constexpr (kPipeC<T, N>) {
-          cands.push_back({1, pipec_ctas_, 1});
-          if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2, 1});
+          cands.push_back({1, pipec_ctas_, 1, 1});
+          if (pipec_ctas_ >= 2 * sms) cands.push_back({1, pipec_ctas_ / 2, 1, 1});
         }
         cpx<T>* c1 = planes_[P_C1];
         cpx<T>* c2 = planes_[P_C2];
@@ -1270,12 +1281,14 @@ class EngineT final : public IEngine {
           pipec_grid_ = cands[i].mode ? cands[i].grid : 0;
           gc_ = cands[i].mode ? GB : cands[i].grid;
           fc_ = cands[i].chunks;
+          wc_ = cands[i].wide;
           launch_passC(c1, c2, c3, c4, 4, nb_);
         });
         tune_c_.clear();
         for (size_t i = 0; i < cands.size(); ++i) {
           TuneRec r{cands[i].mode, cands[i].grid, us[i]};
           r.chunks = cands[i].chunks;
+          r.wide = cands[i].wide;
           tune_c_.push_back(r);
         }
         for (int p : {P_C1, P_C2, P_C3, P_C4})
@@ -1299,7 +1312,7 @@ class EngineT final : public IEngine {
       constexpr int N = decltype(NC)::value;
       constexpr int GA = CfgA<T, N>::G;
       constexpr int GB = Cfg<T, N, PassNT<T, N>::value>::G;
-      int forced[5];
+      int forced[6];
       forced_groups(GA, GB, GB, forced);
       auto argmin = [](const std::vector<TuneRec>& t, const std::function<bool(const TuneRec&)>& ok) {
         size_t k = t.size();
@@ -1378,7 +1391,10 @@ class EngineT final : public IEngine {
       pick_bc(tune_, "R2D3C_PASSB", "per_row_pair", forced[2], passb_mode_, pipeb_grid_, gb_);
       const size_t c0 = pick_bc(tune_c_, "R2D3C_PASSC", "per_column_pair", forced[3], passc_mode_, pipec_grid_, gc_);
       fc_ = forced[4] > 0 ? forced[4] : (c0 < tune_c_.size() ? tune_c_[c0].chunks : 1);
-      if (!kChunkC<T, N>) fc_ = 1;
+      // a forced pass-C group count without a forced team width runs one group per column pair
+      wc_ = forced[5] > 0 ? forced[5] : forced[3] >= 0 ? 1 : (c0 < tune_c_.size() ? tune_c_[c0].wide : 1);
+      if (!kChunkC<T, N>) fc_ = wc_ = 1;
+      if (wc_ > gc_) throw Error(kEINVAL, "R2D3C_GROUPS: pass C team wider than its groups per CTA");
     });
   }
   void set_plan_policy(int policy) override {
@@ -1420,12 +1436,14 @@ class EngineT final : public IEngine {
         snprintf(b, sizeof b, "%s{\"variant\": \"persistent\", \"ctas\": %d, \"us\": %.2f}", i ? ", " : "",
                  tune_c_[i].grid, (double)tune_c_[i].us);
       else
-        snprintf(b, sizeof b, "%s{\"variant\": \"per_column_pair\", \"groups\": %d, \"chunks\": %d, \"us\": %.2f}",
-                 i ? ", " : "", tune_c_[i].grid, tune_c_[i].chunks, (double)tune_c_[i].us);
+        snprintf(b, sizeof b,
+                 "%s{\"variant\": \"per_column_pair\", \"groups\": %d, \"chunks\": %d, \"team\": %d, \"us\": %.2f}",
+                 i ? ", " : "", tune_c_[i].grid, tune_c_[i].chunks, tune_c_[i].wide, (double)tune_c_[i].us);
       r += b;
     }
-    snprintf(b, sizeof b, "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d, \"chunks_c\": %d}",
-             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_, fc_);
+    snprintf(b, sizeof b,
+             "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d, \"chunks_c\": %d, \"team_c\": %d}",
+             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_, fc_, wc_);
     return r + b;
   }
 
@@ -1468,12 +1486,14 @@ class EngineT final : public IEngine {
   int policy_ = 0;      // plan policy (choose_plan)
   int ga_ = 0, fa_ = 1;  // pass A: groups per CTA (0: the config's G), field chunks (autotuned)
   int fc_ = 1;           // pass C: CTAs per column pair (1 or 2, autotuned)
+  int wc_ = 1;           // pass C: groups per column pair sharing its update (autotuned)
   int gb_ = 0, gc_ = 0;  // passes B, C one CTA per row / column pair: groups per CTA (autotuned)
   struct TuneRec {
     int mode, grid;  // pass A: groups, field chunks; B, C: variant, CTAs or groups
     float us;
     int radix = 0;   // pass A: the transform radix
     int chunks = 1;  // pass C: CTAs per column pair
+    int wide = 1;    // pass C: groups per column pair
   };
   // pass A radix chosen per (precision, n), shared by the engines of a process
   static std::map<int, int>& radix_cache() {

@@ -1024,12 +1024,16 @@ __device__ __forceinline__ void passC_update_pairs(cpx<T>* sm, const cpx<T>* hol
                                                    const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out,
                                                    const DevGrid& gd, const StepCoef& sc, T tmp1,
                                                    const cpx<T>* __restrict__ tau5,
-                                                   const cpx<T>* __restrict__ tau6, int chunk = -1) {
+                                                   const cpx<T>* __restrict__ tau6, int chunk = -1,
+                                                   int uidx = -1, int ustride = TPF, bool owner = true) {
   // chunk -1: both outputs; 0: C1 only (v and hold hold the [psi,-k^2 psi]
-  // columns); 1: C2 only (v holds the [psi, vz] columns)
+  // columns); 1: C2 only (v holds the [psi, vz] columns).  The update runs
+  // over ustride threads (thread uidx; default: the group's own TPF), of
+  // which the owner group's results are in sm / hold.
+  if (uidx < 0) uidx = lane;
   const bool do1 = chunk != 1, do2 = chunk != 0;
   cpx<T>* c6s = sm;
-  if (do2) {
+  if (do2 && owner) {
 #pragma unroll
     for (int t = 0; t < NT; ++t)
 #pragma unroll
@@ -1045,13 +1049,13 @@ __device__ __forceinline__ void passC_update_pairs(cpx<T>* sm, const cpx<T>* hol
   constexpr int RB = 2;
   auto ld4 = [](const cpx<T>* base, size_t idx) { return *reinterpret_cast<const F4*>(base + idx); };
 #pragma unroll 1
-  for (int e0 = lane; e0 < total; e0 += RB * TPF) {
+  for (int e0 = uidx; e0 < total; e0 += RB * ustride) {
     F4 a1[RB], a2[RB], p0[RB], f0[RB], v0[RB], g0[RB];
     int col[RB], j0[RB];
     bool keep[RB][2], in[RB][2];
 #pragma unroll
     for (int b = 0; b < RB; ++b) {
-      const int e = e0 + b * TPF;
+      const int e = e0 + b * ustride;
       const int t = e / npc, pi = e % npc;
       const int pr = pi < lo_pairs ? pi : hi_first + (pi - lo_pairs);
       col[b] = kx0 + t;
@@ -1133,7 +1137,7 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out, DevGrid gd,
         const StepCoef* __restrict__ scs, const double* __restrict__ scal, int o,
         const tw_t<T>* __restrict__ tw, Batch bs, const cpx<T>* __restrict__ tau5,
-        const cpx<T>* __restrict__ tau6) {
+        const cpx<T>* __restrict__ tau6, int wide = 1) {
   constexpr int NT = PassNT<T, N>::value;
   using PS = PassSmem<T, N>;
   constexpr bool HOLD = PS::HOLD;
@@ -1153,12 +1157,17 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   const int g = threadIdx.x / C::TPF, lane0 = threadIdx.x % C::TPF;
   cpx<T>* sm = smbase_ + (size_t)g * PS::GROUP_ELEMS;
   cpx<T>* hold = sm + NT * F::SMEM_ELEMS;  // transformed [psi,-k^2 psi] columns (HOLD)
-  const int kx0 = (blockIdx.x * (blockDim.x / C::TPF) + g) * NT;  // groups per CTA: a launch-time choice
+  // wide > 1 (FP32 grids with the held c5): a team of `wide` groups per
+  // column pair; each group transforms (the same values), and the team
+  // shares the RK update, which is the longer part of small grids' chain
+  const int W = (HOLD && sizeof(T) == 4) ? wide : 1;
+  const int team = g / W, member = g % W;
+  const int kx0 = (blockIdx.x * ((blockDim.x / C::TPF) / W) + team) * NT;  // groups per CTA: a launch-time choice
   const size_t oplane = (size_t)gd.nh * N;
   // The RK update at the end reads six spectral planes (eight with the
   // closure tendencies) on this group's columns; they are prefetched into L2
   // now, while the transforms run, so that those reads do not wait for DRAM.
-  if (lane0 < 8) {
+  if (lane0 < 8 && member == 0) {
     const int lane = lane0;
     const cpx<T>* src = lane == 0 ? c1in : lane == 1 ? c2in : lane == 2 ? ps : lane == 3 ? vz
                       : lane == 4 ? fp : lane == 5 ? fz : lane == 6 ? tau5 : tau6;
@@ -1227,8 +1236,10 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
   const StepCoef sc = scs[blockIdx.y];
   const T tmp1 = (T)(scal[blockIdx.y * kScalStride] / (double)o);  // :581
   if constexpr (HOLD && sizeof(T) == 4) {
-    passC_update_pairs<T, N, NT, C::E, C::TPF>(sm, hold, v, lane, kx0, c1in, c2in, ps, vz, fp, fz, c1out, c2out, gd,
-                                                sc, tmp1, tau5, tau6, chunk);
+    cpx<T>* lsm = smbase_ + (size_t)(team * W) * PS::GROUP_ELEMS;  // the team's first group
+    passC_update_pairs<T, N, NT, C::E, C::TPF>(lsm, lsm + NT * F::SMEM_ELEMS, v, lane, kx0, c1in, c2in, ps, vz, fp,
+                                                fz, c1out, c2out, gd, sc, tmp1, tau5, tau6, chunk, member * C::TPF + lane,
+                                                W * C::TPF, member == 0);
   } else if constexpr (HOLD) {
     // c6 joins c5 in shared memory (the transform buffer is free after the
     // last transform; each thread reads back only what it wrote), and the

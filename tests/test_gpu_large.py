@@ -132,7 +132,8 @@ def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
     shapes only: every forced choice steps to the same bits as the tuned one."""
     cp, ps, vz, fp, fz = _case(n, 5)
     out, reps = [], []
-    for forced in (None, "1,6,1,1", "0,1,0,0", "2,3,1,2", "0,1,0,1,2", "1,2,1,2,2", "split"):
+    for forced in (None, "1,6,1,1", "0,1,0,0", "2,3,1,2", "0,1,0,1,2", "1,2,1,2,2", "split", "0,1,0,0,2,4",
+                   "0,1,0,0,2,2"):
         if forced is None:
             monkeypatch.delenv("R2D3C_GROUPS", raising=False)
         elif forced != "split":
@@ -152,6 +153,8 @@ def test_launch_shapes_are_bit_identical(gpu, monkeypatch, n, prec):
     # pass C's C1 and C2 updates split over two CTAs per column pair (FP32)
     assert reps[4]["chunks_c"] == (2 if prec == 1 else 1) and reps[5]["groups_c"] == 2
     assert reps[6]["chosen"] == "split"
+    # teams of groups sharing a column pair's RK update (FP32)
+    assert reps[7]["team_c"] == (4 if prec == 1 else 1) and reps[8]["team_c"] == (2 if prec == 1 else 1)
     for o in out[1:]:
         for u, v in zip(out[0], o):
             np.testing.assert_array_equal(u, v)
