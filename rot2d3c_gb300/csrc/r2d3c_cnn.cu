@@ -1,5 +1,5 @@
 // Learned subgrid closure: a small periodic CNN (6 layers of 3x3 convolution,
-// 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2 channels, GELU between layers) with
+// 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2 channels, GELU (tanh form) between layers) with
 // BF16 operands and FP32 accumulation on the tensor cores, trained with Adam
 // by the kernels of this file.  No counterpart in the reference.
 //
@@ -58,11 +58,24 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks and Gimpel, "Gaussian Error Linear Units",
+// 2016): 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), with the hardware
+// tanh (tanh.approx.f32, about 2^-11 relative error, below the bf16 rounding
+// of every activation); gelu_d is its exact derivative
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;\n" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kGeluA = 0.7978845608028654f, kGeluB = 0.044715f;  // sqrt(2/pi), cubic coefficient
+__device__ __forceinline__ float gelu(float x) {
+  const float t = tanh_hw(kGeluA * fmaf(kGeluB * x, x * x, x));
+  return 0.5f * x * (1.0f + t);
+}
 __device__ __forceinline__ float gelu_d(float x) {
-  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
-  return cdf + x * pdf;
+  const float x2 = x * x;
+  const float t = tanh_hw(kGeluA * fmaf(kGeluB * x, x2, x));
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * kGeluA * fmaf(3.0f * kGeluB, x2, 1.0f);
 }
 
 // ---------------------------------------------------------------------------
@@ -297,8 +310,8 @@ struct TcConv {
   static constexpr bool STAGE_IN_HALO = Y_UNITS + A_UNITS <= HALO_UNITS;
   static constexpr int STAGE_UNITS = STAGE_IN_HALO ? 0 : Y_UNITS + A_UNITS;
   // two halo buffers (the next tile's is copied while this one's runs), the
-  // weights, the output staging, the mbarrier and the TMEM address
-  static constexpr size_t SMEM = (size_t)(2 * HALO_UNITS + W_UNITS + STAGE_UNITS) * 16 + 64;
+  // weights, the output staging, the mbarrier, the TMEM address and the bias
+  static constexpr size_t SMEM = (size_t)(2 * HALO_UNITS + W_UNITS + STAGE_UNITS) * 16 + 16 + 4 * 32;
 };
 
 // halo of tile t into buffer dst (one cp.async commit group; empty when
@@ -334,7 +347,10 @@ k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float*
   uint4* s_stage = s_w + TC::W_UNITS;  // own staging region (STAGE_UNITS)
   unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_stage + TC::STAGE_UNITS);
   unsigned* s_tmem = reinterpret_cast<unsigned*>(s_bar + 1);
+  float* s_bias = reinterpret_cast<float*>(s_bar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // the bias (the last layer's has only its cout_store real channels)
+  if (tid < COUT) s_bias[tid] = bias && tid < cout_store ? bias[tid] : 0.f;
   // weights, already in the K-major UMMA layout: unit (kc, n) = k 8kc..8kc+7 of column n
   for (int i = tid; i < TC::W_UNITS; i += kTcThreads) tc_cp16(s_w + i, wt + (size_t)i * 8);
   tc_commit();
@@ -406,7 +422,7 @@ k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float*
     const int m = warp * 32 + lane;
     float v[COUT];
 #pragma unroll
-    for (int co = 0; co < COUT; ++co) v[co] = __uint_as_float(r[co]) + (bias ? __ldg(bias + co) : 0.f);
+    for (int co = 0; co < COUT; ++co) v[co] = __uint_as_float(r[co]) + s_bias[co];
     if (y && cout_store < COUT) {
       // the network output (2 channels): 8 bytes per pixel straight from registers
 #pragma unroll
