@@ -271,6 +271,15 @@ int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mod
    r2d3c_closure_advance.  No counterpart in the reference. */
 int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int every, int dt_mode,
                                 double cfl_or_dt, double* time, double* dt_last);
+/* The same with the network one step behind the solver and running beside
+   it: the first step of the call takes the tendencies of its own state;
+   step s > 0 takes those of the state before step s - 1, evaluated on a
+   second stream while step s - 1 runs (inside the captured graph, joined
+   before step s).  The network and the RK step are both latency-bound at
+   LES sizes, so the two overlap.  n <= 512, constant forcing.  No
+   counterpart in the reference. */
+int r2d3c_closure_advance_overlapped(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
+                                     double* time, double* dt_last);
 
 /* ---- Regridding (regrid_slices.f90) ------------------------------------ */
 /* The reference's slice regridder applied to a whole field

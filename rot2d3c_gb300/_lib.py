@@ -119,6 +119,7 @@ SIGNATURES = {
     "r2d3c_closure_set_band": (C.c_int, [_P, _P, C.c_int]),
     "r2d3c_closure_advance": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_double, _D, _D]),
     "r2d3c_closure_advance_every": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D]),
+    "r2d3c_closure_advance_overlapped": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_double, _D, _D]),
     "r2d3c_regrid_physical": (C.c_int, [C.c_int, C.c_int, _D, _D]),
     "r2d3c_regrid_physical_dev": (C.c_int, [C.c_int, C.c_int, _P, _P, _P]),
     "r2d3c_regrid_spectral": (C.c_int, [_P, _P]),

@@ -179,13 +179,21 @@ def band_fit(net: CNN, X, Y, idx, n: int, batch: int = 8):
     return np.clip(w, 0.0, 1.0).astype(np.float32)
 
 
-def closure_advance(ctx, net: CNN, nsteps: int, dt_mode: int, cfl_or_dt: float, every: int = 1):
+def closure_advance(ctx, net: CNN, nsteps: int, dt_mode: int, cfl_or_dt: float, every: int = 1,
+                    overlap: bool = False):
     """nsteps LES steps of ctx with the network evaluated before every step
     (``every`` > 1: before every every-th step, its tendencies held in
-    between; one captured CUDA graph per evaluation and its steps).
-    Returns (time, dt of the last step)."""
+    between; one captured CUDA graph per evaluation and its steps).  With
+    ``overlap`` the network runs one step behind, beside the step (step s > 0
+    takes the tendencies of the state before step s - 1;
+    r2d3c_closure_advance_overlapped).  Returns (time, dt of the last step)."""
     t, dtl = C.c_double(), C.c_double()
-    if every == 1:
+    if overlap:
+        if every != 1:
+            raise ValueError("overlap takes every = 1")
+        check(load().r2d3c_closure_advance_overlapped(ctx._h, net._h, nsteps, dt_mode, cfl_or_dt, C.byref(t),
+                                                      C.byref(dtl)), "closure_advance_overlapped")
+    elif every == 1:
         check(load().r2d3c_closure_advance(ctx._h, net._h, nsteps, dt_mode, cfl_or_dt, C.byref(t), C.byref(dtl)),
               "closure_advance")
     else:

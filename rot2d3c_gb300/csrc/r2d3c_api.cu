@@ -1136,8 +1136,10 @@ int r2d3c_closure_advance(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mod
   return r2d3c_closure_advance_every(ctx, cnn, nsteps, 1, dt_mode, cfl_or_dt, time, dt_last);
 }
 
-int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int every, int dt_mode,
-                                double cfl_or_dt, double* time, double* dt_last) {
+namespace {
+// the LES steps of r2d3c_closure_advance_every / _overlapped
+int closure_advance_impl(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int every, bool overlap, int dt_mode,
+                         double cfl_or_dt, double* time, double* dt_last) {
   API_BEGIN
   REQUIRE(ctx && cnn, "NULL argument");
   REQUIRE(nsteps >= 0, "nsteps must be >= 0");
@@ -1151,6 +1153,7 @@ int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int 
   const int n = ctx->p.n;
   REQUIRE(H == n && W == n, "the network's grid must be the context's n x n");
   IEngine* e = ctx->eng.get();
+  REQUIRE(!overlap || e->closure_fused(), "the overlapped LES step takes the fused closure path (n <= 512)");
   if (!ctx->cl_x) {
     cuda_check(cudaMalloc(&ctx->cl_x, sizeof(float) * 8 * (size_t)n * n), "cudaMalloc closure inputs");
     cuda_check(cudaMalloc(&ctx->cl_t, sizeof(float) * 2 * (size_t)n * n), "cudaMalloc closure tendencies");
@@ -1186,14 +1189,17 @@ int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int 
   try {
     if (dt_mode == R2D3C_DT_FIXED) e->set_dt(cfl_or_dt);
     e->set_hook_every(every);
+    e->set_hook_overlap(overlap);
     e->advance(ctx->mc(), nsteps, dt_mode == R2D3C_DT_CFL, cfl_or_dt, nullptr);
   } catch (...) {
     e->set_hook_every(1);
+    e->set_hook_overlap(false);
     e->set_step_hook(nullptr, 0);
     e->set_closure(nullptr, true);
     throw;
   }
   e->set_hook_every(1);
+  e->set_hook_overlap(false);
   e->set_step_hook(nullptr, 0);
   e->set_closure(nullptr, true);
   if (time) *time = e->get_time();
@@ -1201,6 +1207,17 @@ int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int 
   e->sync();
   cnn_check_err(cnn);
   API_END
+}
+}  // namespace
+
+int r2d3c_closure_advance_every(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int every, int dt_mode,
+                                double cfl_or_dt, double* time, double* dt_last) {
+  return closure_advance_impl(ctx, cnn, nsteps, every, false, dt_mode, cfl_or_dt, time, dt_last);
+}
+
+int r2d3c_closure_advance_overlapped(r2d3c_ctx* ctx, r2d3c_cnn* cnn, int nsteps, int dt_mode, double cfl_or_dt,
+                                     double* time, double* dt_last) {
+  return closure_advance_impl(ctx, cnn, nsteps, 1, true, dt_mode, cfl_or_dt, time, dt_last);
 }
 
 int r2d3c_plan_report(r2d3c_ctx* ctx, char* buf, int len) {

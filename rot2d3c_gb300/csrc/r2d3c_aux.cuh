@@ -525,19 +525,26 @@ __global__ void k_spec_sub(const cpx<T>* __restrict__ a, const cpx<T>* __restric
 // Per-shell weights of the learned tendencies: spectral plane a (S = nh * n
 // elements) times w[b], plane b times w[nw + b], b the shell of (kx, ky) by
 // the rule of k_shells (kmn = int(sqrt(ka2) + .5)); shells beyond nw get 0.
+// In place when a_in == a and b_in == b; nw = 0 is a plain copy.
 template <typename T>
-__global__ void k_shell_weight2(cpx<T>* __restrict__ a, cpx<T>* __restrict__ b, DevGrid gd,
+__global__ void k_shell_weight2(const cpx<T>* a_in, const cpx<T>* b_in, cpx<T>* a, cpx<T>* b, DevGrid gd,
                                 const float* __restrict__ w, int nw) {
   const size_t total = (size_t)gd.nh * gd.n;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const cpx<T> u = a_in[i], v = b_in[i];
+    if (nw <= 0) {
+      a[i] = u;
+      b[i] = v;
+      continue;
+    }
     const int kx = (int)(i / gd.n), j = (int)(i % gd.n);
     const int ky = ky_of(j, gd.n);
     // (2b-1)^2 < 4 ka2 < (2b+1)^2  <=>  b = (isqrt(4 ka2) + 1) / 2
     const int bsh = (int)((isqrt_ll(4LL * ((long long)kx * kx + (long long)ky * ky)) + 1) / 2);
     const T fa = bsh < nw ? (T)w[bsh] : (T)0;
     const T fb = bsh < nw ? (T)w[nw + bsh] : (T)0;
-    a[i] = mkc<T>(a[i].x * fa, a[i].y * fa);
-    b[i] = mkc<T>(b[i].x * fb, b[i].y * fb);
+    a[i] = mkc<T>(u.x * fa, u.y * fa);
+    b[i] = mkc<T>(v.x * fb, v.y * fb);
   }
 }
 

@@ -136,6 +136,12 @@ class IEngine {
   // graph of the hook and k steps, and nsteps must be a multiple of k
   // (constant forcing only).  k = 1 is the default.
   virtual void set_hook_every(int k) = 0;
+  // The hook beside the step instead of before it (interval 1, constant
+  // forcing, closure scratch allocated): advance() queues the hook once for
+  // the first step, then every captured step runs the hook for the next step
+  // on a forked stream from the state the step starts from, so step s > 0
+  // takes the hook's result for the state before step s - 1
+  virtual void set_hook_overlap(bool on) = 0;
   virtual void rand_force(const RandForceHost f[2]) = 0;
   // One RK4 step.  cfl_mode: dt from the CFL condition of the current state
   // (fused into the first substep), else the dt already set.  add_time:

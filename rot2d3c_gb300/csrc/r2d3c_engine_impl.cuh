@@ -452,19 +452,51 @@ class EngineT final : public IEngine {
     }
     upload_coefs(mc, cfl);
     const int every = hook_ ? hook_every_ : 1;
+    const bool overlap = hook_ && hook_overlap_;
     if (nsteps % every != 0) throw Error(kEINVAL, "nsteps must be a multiple of the hook interval");
     if (every > 1 && rf) throw Error(kEINVAL, "a hook interval above 1 takes constant forcing");
-    GraphKey key{cfl_mode, rf != nullptr, closure_on_, band_nw_ > 0, hook_ ? hook_id_ : 0ull, every};
+    if (overlap && (every != 1 || rf || !ov_stream_))
+      throw Error(kEINVAL, "an overlapped hook takes interval 1, constant forcing and the closure scratch");
+    // overlapped: the first step of the call takes the hook's result for its
+    // own state, queued here outside the graph
+    if (overlap) hook_(st_);
+    GraphKey key{cfl_mode, rf != nullptr, closure_on_, band_nw_ > 0, hook_ ? hook_id_ : 0ull, every, overlap};
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
       cudaGraph_t g;
       const int before = launches_;
       cuda_check(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal), "BeginCapture");
+      cudaStream_t main = st_;
       try {
-        if (hook_) hook_(st_);
-        for (int k = 0; k < every; ++k) enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr);
+        if (overlap) {
+          // The hook on a forked stream, beside the step: it reads the state
+          // the step starts from (the step's last pass C, which overwrites
+          // it, waits for the inputs kernel) and writes the next step's
+          // tendencies into their own planes, copied (band-weighted) into
+          // the live ones after the join
+          cuda_check(cudaEventRecord(ov_fork_, main), "event fork");
+          cuda_check(cudaStreamWaitEvent(ov_stream_, ov_fork_, 0), "wait fork");
+          st_ = ov_stream_;
+          ov_capture_ = true;
+          hook_(st_);
+          ov_capture_ = false;
+          st_ = main;
+          ov_wait_ = true;
+          enqueue_step(cfl_mode, true, 0, nullptr);
+          ov_wait_ = false;
+          cuda_check(cudaEventRecord(ov_join_, ov_stream_), "event join");
+          cuda_check(cudaStreamWaitEvent(main, ov_join_, 0), "wait join");
+          k_shell_weight2<T><<<elem_blocks(S_), 256, 0, st_>>>(cl_tn_, cl_tn_ + S_, planes_[P_T5], planes_[P_T6], gd_,
+                                                               band_w_, band_nw_);
+          post("k_shell_weight2");
+        } else {
+          if (hook_) hook_(st_);
+          for (int k = 0; k < every; ++k) enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr);
+        }
       } catch (...) {
+        st_ = main;
+        ov_capture_ = ov_wait_ = false;
         cudaStreamEndCapture(st_, &g);
         if (g) cudaGraphDestroy(g);
         throw;
@@ -485,6 +517,7 @@ class EngineT final : public IEngine {
     if (k < 1) throw Error(kEINVAL, "hook interval must be >= 1");
     hook_every_ = k;
   }
+  void set_hook_overlap(bool on) override { hook_overlap_ = on; }
 
   void initial_condition_phys(const std::vector<IcModeHost>& modes) override {
     IcMode* d = nullptr;
@@ -558,13 +591,17 @@ class EngineT final : public IEngine {
   struct GraphKey {
     bool cfl_mode = false, rf = false, closure = false, band = false;
     unsigned long long hook = 0;
-    int every = 1;  // steps per graph (the hook's interval)
+    int every = 1;         // steps per graph (the hook's interval)
+    bool overlap = false;  // the hook beside the step (one step of lag)
     bool same(const GraphKey& o) const {
       return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure && band == o.band && hook == o.hook &&
-             every == o.every;
+             every == o.every && overlap == o.overlap;
     }
   };
   int hook_every_ = 1;
+  bool hook_overlap_ = false;
+  bool ov_capture_ = false;  // the hook is being captured on ov_stream_
+  bool ov_wait_ = false;     // the step being captured waits for the hook's inputs kernel
   static bool batched(int p) { return p <= P_C4; }  // ps, vz, fp, fz, c1 .. c4
 
  public:
@@ -578,6 +615,12 @@ class EngineT final : public IEngine {
     if (cl_t8_) return;
     cl_t8_ = alloc<cpx<T>>(8 * S_);
     cl_r8_ = alloc<T>((size_t)8 * n_ * n_);
+    // the overlapped LES step: its own stream, fork / inputs / join events
+    // and the next step's two tendency planes
+    cl_tn_ = alloc<cpx<T>>(2 * S_);
+    cuda_check(cudaStreamCreateWithFlags(&ov_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaEvent_t* e : {&ov_fork_, &ov_in_, &ov_join_})
+      cuda_check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
   }
   void closure_inputs(float* d_x, bool wait) override {
     // omega = -lap psi = k^2 psi, vz, d/dx and d/dy of psi, omega, vz: the 8
@@ -603,6 +646,8 @@ class EngineT final : public IEngine {
     if (!cl_t8_) throw Error(kESTATE, "closure scratch not allocated (call before any capture)");
     const double s = 1.0 / ((double)n_ * n_);
     launch_closure_cols();
+    // overlapped step: the state has been read, the step may overwrite it
+    if (ov_capture_) cuda_check(cudaEventRecord(ov_in_, st_), "event inputs");
     const Scale8 sc{{-s, s, s, s, -s, -s, s, s}};
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
@@ -625,6 +670,10 @@ class EngineT final : public IEngine {
           y, out_mean, out_sd, cl_t8_, tw_);
       post("k_cnn2_to_rows");
     });
+    if (ov_capture_) {  // the next step's planes; weighted into the live ones after the join
+      launch_colfft<-1>(cl_t8_, cl_tn_, 2 * gd_.nh, cl_tn_ + S_, gd_.nh);
+      return;
+    }
     launch_colfft<-1>(cl_t8_, planes_[P_T5], 2 * gd_.nh, planes_[P_T6], gd_.nh);  // both tendency planes
     band_weight();
     closure_on_ = true;
@@ -698,7 +747,8 @@ class EngineT final : public IEngine {
   // the per-shell weights of set_closure_band on both tendency planes
   void band_weight() {
     if (band_nw_ <= 0) return;
-    k_shell_weight2<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[P_T5], planes_[P_T6], gd_, band_w_, band_nw_);
+    k_shell_weight2<T><<<elem_blocks(S_), 256, 0, st_>>>(planes_[P_T5], planes_[P_T6], planes_[P_T5], planes_[P_T6],
+                                                         gd_, band_w_, band_nw_);
     post("k_shell_weight2");
   }
   // per-run coefficient arrays: nb == 1 takes mc, a batch its run coefficients
@@ -754,6 +804,12 @@ class EngineT final : public IEngine {
     d_ctr_ = nullptr;
     if (hsmall_) cudaFreeHost(hsmall_);
     hsmall_ = nullptr;
+    for (cudaEvent_t* e : {&ov_fork_, &ov_in_, &ov_join_}) {
+      if (*e) cudaEventDestroy(*e);
+      *e = nullptr;
+    }
+    if (ov_stream_) cudaStreamDestroy(ov_stream_);
+    ov_stream_ = nullptr;
     if (st_) cudaStreamDestroy(st_);
     st_ = nullptr;
   }
@@ -897,6 +953,7 @@ class EngineT final : public IEngine {
         k_randforce_seq<T><<<1, 1, 0, st_>>>(pbase_[P_FP], pbase_[P_FZ], scal_base_, d_rf_, d_ctr_);
         post("k_randforce_seq");
       }
+      if (o == 1 && ov_wait_) cuda_check(cudaStreamWaitEvent(st_, ov_in_, 0), "wait inputs");
       timed(2, [&] { launch_passC(in1, in2, out1, out2, o, nb_); });
     }
   }
@@ -1474,6 +1531,9 @@ class EngineT final : public IEngine {
   float* band_w_ = nullptr;  // per-shell tendency weights (set_closure_band)
   int band_nw_ = 0;
   T* cl_r8_ = nullptr;
+  cpx<T>* cl_tn_ = nullptr;  // the overlapped LES step's next tendencies (2 planes)
+  cudaStream_t ov_stream_ = nullptr;
+  cudaEvent_t ov_fork_ = nullptr, ov_in_ = nullptr, ov_join_ = nullptr;
   std::function<void(cudaStream_t)> hook_;
   unsigned long long hook_id_ = 0;
   int pipeb_ctas_ = 0;  // resident CTAs of the pipelined pass B (whole device)

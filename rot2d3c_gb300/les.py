@@ -221,7 +221,7 @@ def train_network(ds, train_steps=3000, batch=32, lr=1e-3, seed=1):
 
 
 def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near_cutoff",), time_dns=True,
-             val_loss=None, skill_gate=0.9, every=1):
+             val_loss=None, skill_gate=0.9, every=1, overlap=False):
     """Stage 3: from every held-out start, the plain coarse solver, the
     hyperviscous fallback and one LES per band rule (``bands``, see
     band_weights) advance les_steps CFL steps; spectra and fluxes averaged
@@ -232,7 +232,9 @@ def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near
     ``val_loss`` (standardised: 1 = predicting the mean) is not below
     ``skill_gate`` has no skill to apply: its LES runs as the hyperviscous
     fallback, the closure's stated fallback.  every: the network is
-    evaluated before every every-th LES step (its tendencies held between)."""
+    evaluated before every every-th LES step (its tendencies held between);
+    overlap: the network runs one step behind, beside the step
+    (closure_advance with overlap)."""
     import torch
     cfg = ds["cfg"]
     nc, nu, hnu, omega, cfl = cfg["nc"], cfg["nu"], cfg["hnu"], cfg["omega"], cfg["cfl"]
@@ -275,7 +277,7 @@ def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near
             t_end = ds["snap_t"][si]
             for s in range(0, les_steps, spec_every):
                 if name in les_names and not gated:
-                    t_end, _ = closure_advance(c, net, spec_every, DT_CFL, cfl, every=every)
+                    t_end, _ = closure_advance(c, net, spec_every, DT_CFL, cfl, every=every, overlap=overlap)
                 else:
                     t_end, _ = c.advance(spec_every, DT_CFL, cfl)
                 if s + spec_every > les_steps // 2:
@@ -329,7 +331,8 @@ def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near
 
 def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=10, spinup=2000,
                    train_steps=3000, batch=32, lr=1e-3, les_steps=4000, cfl=0.5, seed=1,
-                   fallback_nn=4, spec_every=50, hnu=0.1, starts=4, band="near_cutoff", compare_bands=(), every=1):
+                   fallback_nn=4, spec_every=50, hnu=0.1, starts=4, band="near_cutoff", compare_bands=(), every=1,
+                   overlap=False):
     """The three stages; returns a dict of timings and errors.
 
     nf, nc: DNS and LES grids; nu: viscosity of both (nn = 1); omega:
@@ -340,7 +343,7 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
     halves are averaged for the spectra (one spectrum every spec_every
     steps); band: the band rule of the LES tendencies (band_weights);
     every: network evaluations every that many LES steps (spec_every must
-    be a multiple);
+    be a multiple); overlap: the network one step behind, beside the step;
     compare_bands: further LES band rules run for comparison.  The fallback
     run replaces the viscosity by a hyperviscosity of order fallback_nn with
     the damping rate 20 nu k_c^2 at the cutoff k_c = nc/3.
@@ -350,13 +353,14 @@ def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=1
                      seed=seed, hnu=hnu, starts=starts)
     net, training = train_network(ds, train_steps=train_steps, batch=batch, lr=lr, seed=seed)
     ev = evaluate(ds, net, les_steps=les_steps, spec_every=spec_every, fallback_nn=fallback_nn,
-                  bands=(band,) + tuple(compare_bands), val_loss=training["val_loss"], every=every)
+                  bands=(band,) + tuple(compare_bands), val_loss=training["val_loss"], every=every,
+                  overlap=overlap)
     name = _rule_name(band)
     err = {"les": ev["spectrum_error"][name], "plain": ev["spectrum_error"]["plain"],
            "fallback": ev["spectrum_error"]["fallback"]}
     err.update({k: v for k, v in ev["spectrum_error"].items() if k not in (name, "plain", "fallback")})
     les = dict(ev["les"], gpu_s=ev["les"]["gpu_s"][name], band=band if isinstance(band, (str, type(None)))
-               else list(band), network_every=every)
+               else list(band), network_every=every, network_overlap=overlap)
     ds["fine"].destroy()
     ds["coarse"].destroy()
     net.destroy()

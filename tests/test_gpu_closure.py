@@ -193,3 +193,55 @@ def test_network_every_second_step_equals_the_step_by_step_loop(gpu, prec):
             np.testing.assert_array_equal(u, v)
     with pytest.raises(gpu.R2D3CError):
         closure_advance(b, net, 3, gpu.DT_FIXED, 1e-3, every=2)
+
+
+@pytest.mark.parametrize("prec,band", [(0, False), (1, False), (1, True)])
+def test_overlapped_les_steps_equal_the_lagged_step_by_step_loop(gpu, prec, band):
+    """r2d3c_closure_advance_overlapped (the network for the next step on a
+    second stream beside the current step, inside one captured graph): the
+    first step of a call takes the tendencies of its own state, step s > 0
+    those of the state before step s - 1.  Bit-identical to that schedule
+    made one call at a time, in both dt modes, with and without per-shell
+    weights (applied to the next tendencies after the join)."""
+    import torch
+    from rot2d3c_gb300.closure import CNN, closure_advance, closure_inputs, set_band, set_tendency
+    n = 32
+    _, cp = params(n, omega=1.0, nu=2e-3, nuv=2e-3, hnu=0.1, hnuv=0.1, iflow=0)
+    g, ps, vz = random_state(n, 71, amp=20.0)
+    fp, fz = random_forcing(g, 72, 2.0, 4.0)
+    net = CNN(n, n, 1, 13)
+    net.set_normalization(np.zeros(8), np.full(8, 50.0), np.zeros(2), np.full(2, 5.0))
+    for mode, val in ((gpu.DT_CFL, 0.4), (gpu.DT_FIXED, 1e-3)):
+        a = gpu.Context(cp, prec)
+        b = gpu.Context(cp, prec)
+        for c in (a, b):
+            c.set_state(ps, vz)
+            c.set_forcing(fp, fz)
+            c.set_time(0.0)
+            if band:
+                set_band(c, np.linspace(1.0, 0.2, 2 * 12, dtype=np.float32).reshape(2, 12))
+        x = torch.empty((1, n, n, 8), dtype=torch.float32, device="cuda")
+        t = torch.empty((1, n, n, 2), dtype=torch.float32, device="cuda")
+        tn = torch.empty_like(t)
+        for nsteps in (3, 2):  # two calls: each starts from its own state's tendencies
+            closure_inputs(a, x[0])
+            net.forward(x, 1, t)
+            for _ in range(nsteps):
+                closure_inputs(a, x[0])
+                net.forward(x, 1, tn)
+                set_tendency(a, t[0])
+                ta, _ = a.advance(1, mode, val)
+                t.copy_(tn)
+        set_tendency(a, None)
+        tb, _ = closure_advance(b, net, 3, mode, val, overlap=True)
+        tb, _ = closure_advance(b, net, 2, mode, val, overlap=True)
+        assert ta == tb
+        for u, v in zip(a.get_state(), b.get_state()):
+            np.testing.assert_array_equal(u, v)
+        # plain steps afterwards: the tendencies are off on both
+        a.advance(2, mode, val)
+        b.advance(2, mode, val)
+        for u, v in zip(a.get_state(), b.get_state()):
+            np.testing.assert_array_equal(u, v)
+    with pytest.raises(ValueError):
+        closure_advance(b, net, 2, gpu.DT_FIXED, 1e-3, every=2, overlap=True)
