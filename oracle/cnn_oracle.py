@@ -1,13 +1,14 @@
 """Float64 NumPy reference of the closure CNN (TEST INFRASTRUCTURE ONLY).
 
 Six periodic 3x3 convolutions 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2 with
-GELU (tanh form) between them, NHWC layout, MSE loss, and the hand-derived
+GELU (erf form) between them, NHWC layout, MSE loss, and the hand-derived
 backward pass.  With ``emulate=True`` the inputs, weights, inter-layer
 activations and back-propagated gradients are rounded to bfloat16 where the
 GPU kernels round them, so the comparison isolates accumulation order.
 The network has no counterpart in the reference program.
 """
 import numpy as np
+from scipy.special import erf
 
 CIN = [8, 32, 32, 32, 32, 32]
 COUT = [32, 32, 32, 32, 32, 2]
@@ -50,19 +51,12 @@ def conv_t(g, w):
     return x
 
 
-# GELU in its tanh form (Hendrycks and Gimpel, "Gaussian Error Linear Units",
-# 2016): 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), as the GPU kernels
-# evaluate it (there with the hardware tanh approximation)
-_GA, _GB = np.sqrt(2.0 / np.pi), 0.044715
-
-
 def gelu(x):
-    return 0.5 * x * (1.0 + np.tanh(_GA * (x + _GB * x ** 3)))
+    return 0.5 * x * (1.0 + erf(x / np.sqrt(2.0)))
 
 
 def gelu_d(x):
-    t = np.tanh(_GA * (x + _GB * x ** 3))
-    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * _GA * (1.0 + 3.0 * _GB * x * x)
+    return 0.5 * (1.0 + erf(x / np.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / np.sqrt(2.0 * np.pi)
 
 
 def forward(params, x, emulate=True):

@@ -1,5 +1,5 @@
 // Learned subgrid closure: a small periodic CNN (6 layers of 3x3 convolution,
-// 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2 channels, GELU (tanh form) between layers) with
+// 8 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2 channels, GELU between layers) with
 // BF16 operands and FP32 accumulation on the tensor cores, trained with Adam
 // by the kernels of this file.  No counterpart in the reference.
 //
@@ -58,24 +58,11 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// GELU in its tanh form (Hendrycks and Gimpel, "Gaussian Error Linear Units",
-// 2016): 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), with the hardware
-// tanh (tanh.approx.f32, about 2^-11 relative error, below the bf16 rounding
-// of every activation); gelu_d is its exact derivative
-__device__ __forceinline__ float tanh_hw(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;\n" : "=f"(y) : "f"(x));
-  return y;
-}
-constexpr float kGeluA = 0.7978845608028654f, kGeluB = 0.044715f;  // sqrt(2/pi), cubic coefficient
-__device__ __forceinline__ float gelu(float x) {
-  const float t = tanh_hw(kGeluA * fmaf(kGeluB * x, x * x, x));
-  return 0.5f * x * (1.0f + t);
-}
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_d(float x) {
-  const float x2 = x * x;
-  const float t = tanh_hw(kGeluA * fmaf(kGeluB * x, x2, x));
-  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * kGeluA * fmaf(3.0f * kGeluB, x2, 1.0f);
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
+  return cdf + x * pdf;
 }
 
 // ---------------------------------------------------------------------------
