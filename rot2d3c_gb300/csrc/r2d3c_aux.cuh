@@ -548,12 +548,60 @@ __global__ void k_shell_weight2(const cpx<T>* a_in, const cpx<T>* b_in, cpx<T>* 
   }
 }
 
+// The forward y-transform of the two tendency planes (columns 0 .. nh-1 of
+// `in` into a, nh .. 2nh-1 into b, as k_colfft with a split output), each
+// element times the band weight of its shell (the rule and the multiply of
+// k_shell_weight2): the transform and the weighting of the captured LES
+// step in one launch, the same bits as the two launches.
+template <typename T, int N>
+__global__ void __launch_bounds__(Cfg<T, N>::THREADS)
+k_colfft_band2(const cpx<T>* __restrict__ in, cpx<T>* __restrict__ a, cpx<T>* __restrict__ b, int nh,
+               const tw_t<T>* __restrict__ tw, const float* __restrict__ w, int nw) {
+  using C = Cfg<T, N>;
+  using F = typename C::FFT;
+  R2D3C_SMEM_DECL
+  const int g = threadIdx.x / C::TPF, lane = threadIdx.x % C::TPF;
+  cpx<T>* sm = smbase_ + (size_t)g * F::SMEM_ELEMS;
+  const int col = blockIdx.x * (blockDim.x / C::TPF) + g;  // groups per CTA: a launch-time choice
+  const bool ok = col < 2 * nh;
+  cpx<T> v[1][C::E];
+#pragma unroll
+  for (int q = 0; q < C::E; ++q) v[0][q] = ok ? in[(size_t)col * N + lane + q * C::TPF] : czero<T>();
+  F::template run<-1>(v, lane, sm, tw);
+  if (ok) {
+    const bool second = col >= nh;
+    const int kx = second ? col - nh : col;
+    cpx<T>* dst = (second ? b : a) + (size_t)kx * N;
+    const float* wp = w + (second ? nw : 0);
+#pragma unroll
+    for (int q = 0; q < C::E; ++q) {
+      const int j = lane + q * C::TPF, ky = ky_of(j, N);
+      const int bsh = (int)((isqrt_ll(4LL * ((long long)kx * kx + (long long)ky * ky)) + 1) / 2);
+      const T f = bsh < nw ? (T)wp[bsh] : (T)0;
+      dst[j] = mkc<T>(v[0][q].x * f, v[0][q].y * f);
+    }
+  }
+}
+
+// (float)(v * s) for the closure's scales s = +-1/n^2, powers of two (n is
+// one): the FP32 product is exact (or the same correctly rounded subnormal)
+// and equal to the FP64 product rounded to FP32, so the FP32 path keeps its
+// conversions off the FP64 pipe
+template <typename T>
+__device__ __forceinline__ float scale_to_float(T v, double s) {
+  if constexpr (sizeof(T) == 4) {
+    return v * (float)s;
+  } else {
+    return (float)(v * s);
+  }
+}
+
 // out[p*nch + ch] = r[p] * s  (real plane -> one channel of an FP32 NHWC tensor)
 template <typename T>
 __global__ void k_to_channel(const T* __restrict__ r, size_t count, double s, float* __restrict__ out, int nch,
                              int ch) {
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < count; p += (size_t)gridDim.x * blockDim.x)
-    out[p * nch + ch] = (float)((double)r[p] * s);
+    out[p * nch + ch] = scale_to_float(r[p], s);
 }
 
 // Spectral field c (0..7) of the closure's inputs at (kx, ky) from psi (x)
@@ -619,7 +667,7 @@ __global__ void k_to_channels8(const T* __restrict__ r8, size_t count, Scale8 s,
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < count; p += (size_t)gridDim.x * blockDim.x) {
     float o[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) o[c] = (float)((double)r8[c * count + p] * s.v[c]);
+    for (int c = 0; c < 8; ++c) o[c] = scale_to_float(r8[c * count + p], s.v[c]);
     reinterpret_cast<float4*>(out + p * 8)[0] = make_float4(o[0], o[1], o[2], o[3]);
     reinterpret_cast<float4*>(out + p * 8)[1] = make_float4(o[4], o[5], o[6], o[7]);
   }
@@ -693,7 +741,7 @@ k_rows_to_cnn8(const cpx<T>* __restrict__ tin, Scale8 s, const float* __restrict
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const T val = reinterpret_cast<const T*>(smbase_ + (size_t)(c + h) * F::SMEM_ELEMS)[p];
-        const float x = (float)((double)val * s.v[c + h]);
+        const float x = scale_to_float(val, s.v[c + h]);
         o[h] = (x - mean[c + h]) / sd[c + h];
       }
       const __nv_bfloat162 b2 = __floats2bfloat162_rn(o[0], o[1]);

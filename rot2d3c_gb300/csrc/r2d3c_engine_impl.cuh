@@ -460,7 +460,11 @@ class EngineT final : public IEngine {
     // overlapped: the first step of the call takes the hook's result for its
     // own state, queued here outside the graph
     if (overlap) hook_(st_);
-    GraphKey key{cfl_mode, rf != nullptr, closure_on_, band_nw_ > 0, hook_ ? hook_id_ : 0ull, every, overlap};
+    // pass C with the next substep's pass A: the graph's steps start at pass
+    // B, and the first pass A of the call is queued here
+    const bool fuse = fuse_ca();
+    if (fuse) launch_passA(pbase_[P_PS], pbase_[P_VZ], tf_, nb_);
+    GraphKey key{cfl_mode, rf != nullptr, closure_on_, band_nw_ > 0, hook_ ? hook_id_ : 0ull, every, overlap, fuse};
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
@@ -483,7 +487,7 @@ class EngineT final : public IEngine {
           ov_capture_ = false;
           st_ = main;
           ov_wait_ = true;
-          enqueue_step(cfl_mode, true, 0, nullptr);
+          enqueue_step(cfl_mode, true, 0, nullptr, fuse);
           ov_wait_ = false;
           cuda_check(cudaEventRecord(ov_join_, ov_stream_), "event join");
           cuda_check(cudaStreamWaitEvent(main, ov_join_, 0), "wait join");
@@ -492,7 +496,7 @@ class EngineT final : public IEngine {
           post("k_shell_weight2");
         } else {
           if (hook_) hook_(st_);
-          for (int k = 0; k < every; ++k) enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr);
+          for (int k = 0; k < every; ++k) enqueue_step(cfl_mode, true, rf ? -1 : 0, nullptr, fuse);
         }
       } catch (...) {
         st_ = main;
@@ -593,13 +597,15 @@ class EngineT final : public IEngine {
     unsigned long long hook = 0;
     int every = 1;         // steps per graph (the hook's interval)
     bool overlap = false;  // the hook beside the step (one step of lag)
+    bool fuse = false;     // pass C carries the next substep's pass A
     bool same(const GraphKey& o) const {
       return cfl_mode == o.cfl_mode && rf == o.rf && closure == o.closure && band == o.band && hook == o.hook &&
-             every == o.every && overlap == o.overlap;
+             every == o.every && overlap == o.overlap && fuse == o.fuse;
     }
   };
   int hook_every_ = 1;
   bool hook_overlap_ = false;
+  bool fuse_ca_on_ = true;  // R2D3C_FUSE_CA
   bool ov_capture_ = false;  // the hook is being captured on ov_stream_
   bool ov_wait_ = false;     // the step being captured waits for the hook's inputs kernel
   static bool batched(int p) { return p <= P_C4; }  // ps, vz, fp, fz, c1 .. c4
@@ -636,6 +642,14 @@ class EngineT final : public IEngine {
     k_to_channels8<T><<<elem_blocks(cnt), 256, 0, st_>>>(cl_r8_, cnt, sc, d_x);
     post("k_to_channels8");
     if (wait) sync();
+  }
+  // pass C carries the next substep's pass A inside advance(): FP32 grids up
+  // to 512, one run, no const_inj, one CTA (or team) per column pair;
+  // R2D3C_FUSE_CA=0 keeps the separate pass A
+  bool fuse_ca() const {
+    bool ok = false;
+    dispatch_n(n_, [&](auto NC) { ok = kFuseCA<T, decltype(NC)::value>; });
+    return ok && fuse_ca_on_ && nb_ == 1 && !ci_on_ && passc_mode_ == 0;
   }
   bool closure_fused() const override {
     bool ok = false;
@@ -674,8 +688,18 @@ class EngineT final : public IEngine {
       launch_colfft<-1>(cl_t8_, cl_tn_, 2 * gd_.nh, cl_tn_ + S_, gd_.nh);
       return;
     }
-    launch_colfft<-1>(cl_t8_, planes_[P_T5], 2 * gd_.nh, planes_[P_T6], gd_.nh);  // both tendency planes
-    band_weight();
+    if (band_nw_ > 0) {  // both tendency planes, transformed and band-weighted in one launch
+      dispatch_n(n_, [&](auto NC) {
+        constexpr int N = decltype(NC)::value;
+        using C = Cfg<T, N>;
+        const int ncols = 2 * gd_.nh, g = fft_groups(ncols, C::G);
+        k_colfft_band2<T, N><<<(ncols + g - 1) / g, C::TPF * g, g * C::FFT::SMEM_BYTES, st_>>>(
+            cl_t8_, planes_[P_T5], planes_[P_T6], gd_.nh, tw_, band_w_, band_nw_);
+        post("k_colfft_band2");
+      });
+    } else {
+      launch_colfft<-1>(cl_t8_, planes_[P_T5], 2 * gd_.nh, planes_[P_T6], gd_.nh);  // both tendency planes
+    }
     closure_on_ = true;
   }
   void set_closure_band(const float* w, int nw) override {
@@ -909,7 +933,10 @@ class EngineT final : public IEngine {
   // rf_mode: 0 none, 1 single args (rf), -1 sequence from the device array.
   // All nb_ runs advance together (blockIdx.y = run); forcing draws and
   // const_inj are single-run features.
-  void enqueue_step(bool cfl_mode, bool add_time, int rf_mode, const RandForceHost* rf) {
+  // fuse: pass A of every substep was queued before (by the previous
+  // substep's pass C, or by advance() for the first), and every pass C
+  // carries the next substep's pass A (fuse_ca())
+  void enqueue_step(bool cfl_mode, bool add_time, int rf_mode, const RandForceHost* rf, bool fuse = false) {
     if (nb_ > 1 && (rf_mode != 0 || ci_on_)) throw Error(kEINVAL, "batched runs take constant forcing");
     cpx<T>* ps = pbase_[P_PS];
     cpx<T>* vz = pbase_[P_VZ];
@@ -931,7 +958,7 @@ class EngineT final : public IEngine {
         enqueue_const_inj(in1, pin1, P_FP, 1, ci_fp0_);
         enqueue_const_inj(in2, pin2, P_FZ, 0, ci_fz0_);
       }
-      timed(0, [&] { launch_passA(in1, in2, tf_, nb_); });
+      if (!fuse) timed(0, [&] { launch_passA(in1, in2, tf_, nb_); });
       if (o == 4 && cfl_mode) {
         cuda_check(cudaMemsetAsync(enc_base_, 0, sizeof(unsigned long long) * kScalStride * nb_, st_),
                    "memset cfl");
@@ -954,7 +981,7 @@ class EngineT final : public IEngine {
         post("k_randforce_seq");
       }
       if (o == 1 && ov_wait_) cuda_check(cudaStreamWaitEvent(st_, ov_in_, 0), "wait inputs");
-      timed(2, [&] { launch_passC(in1, in2, out1, out2, o, nb_); });
+      timed(2, [&] { launch_passC(in1, in2, out1, out2, o, nb_, fuse); });
     }
   }
 
@@ -1094,7 +1121,8 @@ class EngineT final : public IEngine {
       }
     });
   }
-  void launch_passC(const cpx<T>* c1in, const cpx<T>* c2in, cpx<T>* c1out, cpx<T>* c2out, int o, int nb) {
+  void launch_passC(const cpx<T>* c1in, const cpx<T>* c2in, cpx<T>* c1out, cpx<T>* c2out, int o, int nb,
+                    bool fuse = false) {
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
       constexpr int NT = PassNT<T, N>::value;
@@ -1116,6 +1144,10 @@ class EngineT final : public IEngine {
       }
       if (!persistent) {  // one CTA (group) per column pair
         auto k = k_passC<T, N>;
+        if constexpr (kFuseCA<T, N>) {
+          if (fuse) k = k_passC<T, N, true>;
+        }
+        if (fuse && !kFuseCA<T, N>) throw Error(kESTATE, "pass C carries pass A only for FP32 n <= 512");
         const int groups = (gd_.M + NT - 1) / NT;
         const int g = gc_ ? gc_ : C::G;  // groups per CTA: autotuned
         // the C1 and C2 updates of a column pair in one CTA or two, and
@@ -1125,7 +1157,8 @@ class EngineT final : public IEngine {
         const dim3 grid((groups + teams - 1) / teams, nb, kChunkC<T, N> ? fc_ : 1);
         k<<<grid, C::TPF * g, g * PassSmem<T, N>::GROUP_ELEMS * sizeof(cpx<T>), st_>>>(pb_, c1in, c2in, pbase_[P_PS], pbase_[P_VZ],
                                                            pbase_[P_FP], pbase_[P_FZ], c1out, c2out, gd_, d_sc_,
-                                                           scal_base_, o, tw_, batch(), t5, t6, w);
+                                                           scal_base_, o, tw_, batch(), t5, t6, w,
+                                                           fuse ? tf_ : nullptr, fuse ? tw_a_ : nullptr);
         post("k_passC");
       }
     });
@@ -1144,6 +1177,7 @@ class EngineT final : public IEngine {
       set_smem_attr(k_rowr2c<T, N>, sm);
       set_smem_attr(k_cnn2_to_rows<T, N>, sm);
       set_smem_attr(k_closure_cols<T, N>, sm);
+      set_smem_attr(k_colfft_band2<T, N>, sm);
       if constexpr (RowsCnn<T, N>::OK) set_smem_attr(k_rows_to_cnn8<T, N>, RowsCnn<T, N>::SMEM);
       constexpr size_t smh = PassSmem<T, N>::SMEM;
       set_smem_attr(k_passA<T, N>, CfgA<T, N>::SMEM);
@@ -1155,6 +1189,7 @@ class EngineT final : public IEngine {
         set_smem_attr(k_passB_split<T, N, false>, SplitB<T, N>::SMEM);
       }
       set_smem_attr(k_passC<T, N>, smh);
+      if constexpr (kFuseCA<T, N>) set_smem_attr(k_passC<T, N, true>, smh);
       if constexpr (kPipeC<T, N>) {
         set_smem_attr(k_passC_pipe<N>, PipeC<N>::SMEM);
         cuda_check(cudaFuncSetAttribute(k_passC_pipe<N>, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -1364,6 +1399,10 @@ class EngineT final : public IEngine {
   // with the config's groups per CTA or persistent.  The environment
   // overrides (R2D3C_PASSB, R2D3C_PASSC, R2D3C_GROUPS) apply to both.
   void choose_plan() {
+    if (const char* e = std::getenv("R2D3C_FUSE_CA")) {
+      if (std::strcmp(e, "0") != 0 && std::strcmp(e, "1") != 0) throw Error(kEINVAL, "R2D3C_FUSE_CA must be 0 or 1");
+      fuse_ca_on_ = e[0] == '1';
+    }
     if (tune_a_.empty()) return;
     dispatch_n(n_, [&](auto NC) {
       constexpr int N = decltype(NC)::value;
@@ -1499,8 +1538,10 @@ class EngineT final : public IEngine {
       r += b;
     }
     snprintf(b, sizeof b,
-             "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d, \"chunks_c\": %d, \"team_c\": %d}",
-             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_, fc_, wc_);
+             "], \"chosen_c\": \"%s\", \"ctas_c\": %d, \"groups_c\": %d, \"chunks_c\": %d, \"team_c\": %d, "
+             "\"fused_ca\": %s}",
+             passc_mode_ ? "persistent" : "per_column_pair", passc_mode_ ? pipec_grid_ : 0, gc_, fc_, wc_,
+             fuse_ca() ? "true" : "false");
     return r + b;
   }
 

@@ -22,6 +22,8 @@
 //      RK update with Coriolis coupling and forcing (Rot2D3C.para.f90:578-599).
 #pragma once
 
+#include <type_traits>
+
 #include "r2d3c_fft.cuh"
 
 namespace r2d3c {
@@ -1130,14 +1132,22 @@ __device__ __forceinline__ void passC_update_pairs(cpx<T>* sm, const cpx<T>* hol
   }
 }
 
-template <typename T, int N>
+// Pass C with ATAIL: the next substep's pass A on the same column pairs, in
+// the same launch (FP32, n <= 512): the team that updated a column pair
+// reads back the state it has just written (c1out: psi, c2out: vz) and
+// derivative-transforms it into the mixed planes atf, each team group
+// taking other fields, with the per-field arithmetic of k_passA (the same
+// transform configuration and twiddle table `twa`), so the results are
+// bit-identical to the separate pass A.
+template <typename T, int N, bool ATAIL = false>
 __global__ void __launch_bounds__(Cfg<T, N, PassNT<T, N>::value>::THREADS, 1)
 k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
         const cpx<T>* ps, const cpx<T>* vz, const cpx<T>* __restrict__ fp,
         const cpx<T>* __restrict__ fz, cpx<T>* c1out, cpx<T>* c2out, DevGrid gd,
         const StepCoef* __restrict__ scs, const double* __restrict__ scal, int o,
         const tw_t<T>* __restrict__ tw, Batch bs, const cpx<T>* __restrict__ tau5,
-        const cpx<T>* __restrict__ tau6, int wide = 1) {
+        const cpx<T>* __restrict__ tau6, int wide = 1, cpx<T>* __restrict__ atf = nullptr,
+        const tw_t<T>* __restrict__ twa = nullptr) {
   constexpr int NT = PassNT<T, N>::value;
   using PS = PassSmem<T, N>;
   constexpr bool HOLD = PS::HOLD;
@@ -1240,6 +1250,66 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
     passC_update_pairs<T, N, NT, C::E, C::TPF>(lsm, lsm + NT * F::SMEM_ELEMS, v, lane, kx0, c1in, c2in, ps, vz, fp,
                                                 fz, c1out, c2out, gd, sc, tmp1, tau5, tau6, chunk, member * C::TPF + lane,
                                                 W * C::TPF, member == 0);
+    if constexpr (ATAIL) {
+      using CA = CfgA<T, N>;
+      static_assert(NT == 2 && std::is_same<typename CA::FFT, F>::value && CA::TPF == C::TPF,
+                    "pass A's transform configuration is pass C's");
+      // the team's update stores (and its reads of the shared staging) are
+      // done: the state written is visible to the whole CTA
+      __syncthreads();
+      // fields 0-3 from the new psi (C1), 4-5 from the new vz (C2); a CTA of
+      // a chunked launch takes its own update's fields.  Every group runs the
+      // same number of transforms (their barriers are CTA-wide above 32
+      // threads per transform); a group without a field transforms zeros and
+      // stores nothing.
+      const int fb = chunk == 1 ? 4 : 0, fe = chunk == 0 ? 4 : 6;
+      const int rounds = (fe - fb + W - 1) / W;
+      const size_t plane = (size_t)gd.M * N;
+      cpx<T>* asm_ = smbase_ + (size_t)g * PS::GROUP_ELEMS;  // this group's transform buffers
+#pragma unroll 1
+      for (int r = 0; r < rounds; ++r) {
+        const int f = fb + member + r * W;
+        const bool act = f < fe;
+        const cpx<T>* sp = f < 4 ? c1out : c2out;
+        cpx<T> a[NT][C::E];
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+          const int col = kx0 + t;
+#pragma unroll
+          for (int q = 0; q < C::E; ++q) {
+            const int ky = ky_of(lane + q * C::TPF, N);
+            const bool in = act && col < gd.M && (ky <= gd.L && -ky <= gd.L) && col * col + ky * ky <= gd.kmaxi;
+            cpx<T> x = in ? sp[(size_t)col * N + lane + q * C::TPF] : czero<T>();
+            // (0,k)*(x,y) = (-k*y, k*x): derivk2 dir 1 (k = kx) / dir 2 (k = ky)
+            const T k = (f & 1) ? (T)ky : (T)col;
+            if (f == 2 || f == 3) {
+              const T m = -(T)(col * col + ky * ky);  // laplak2: -ka2*a
+              x = mkc<T>(m * x.x, m * x.y);
+            }
+            a[t][q] = mkc<T>(-k * x.y, k * x.x);
+          }
+        }
+        F::template run<+1>(a, lane, asm_, twa);
+        // lanes (2p, 2p+1) hold rows y = 2p, 2p+1 of columns kx0, kx0+1: one
+        // swap, then each lane writes one column's row pair (16 bytes)
+        const bool odd = lane & 1;
+        const int kx = kx0 + (odd ? 1 : 0);
+        cpx<T>* dst = atf + (size_t)(act ? f : 0) * plane;
+#pragma unroll
+        for (int q = 0; q < C::E; ++q) {
+          const cpx<T> give = odd ? a[0][q] : a[1][q];
+          cpx<T> got;
+          got.x = __shfl_xor_sync(0xffffffffu, give.x, 1);
+          got.y = __shfl_xor_sync(0xffffffffu, give.y, 1);
+          const int y = (lane + q * C::TPF) & ~1;
+          if (act && kx < gd.M) {
+            const cpx<T> lo = odd ? got : a[0][q];
+            const cpx<T> hi = odd ? a[1][q] : got;
+            *reinterpret_cast<float4*>(dst + mix_idx<N, 2>(kx, y, gd.M)) = make_float4(lo.x, lo.y, hi.x, hi.y);
+          }
+        }
+      }
+    }
   } else if constexpr (HOLD) {
     // c6 joins c5 in shared memory (the transform buffer is free after the
     // last transform; each thread reads back only what it wrote), and the
@@ -1342,6 +1412,11 @@ struct PipeC {
 // = 2) where it holds c5 in shared memory and updates row pairs (FP32)
 template <typename T, int N>
 constexpr bool kChunkC = sizeof(T) == 4 && PassSmem<T, N>::HOLD;
+// pass C carries the next substep's pass A (k_passC<T, N, true>): FP32 grids
+// whose pass A and pass C share one transform configuration
+template <typename T, int N>
+constexpr bool kFuseCA = sizeof(T) == 4 && N <= 512 && PassNT<T, N>::value == 2 && PassSmem<T, N>::HOLD &&
+                         !kAltRadixA<T, N> && PassAE<T, N>::value == Cfg<T, N>::E;
 template <typename T, int N>
 constexpr bool kPipeC = sizeof(T) == 4 && PassNT<T, N>::value == 2 && PassSmem<T, N>::HOLD &&
                         PipeC<N>::THREADS >= 64 && PipeC<N>::THREADS <= 512;

@@ -190,3 +190,48 @@ def test_fp32_pass_a_radices_stay_within_the_fp32_bound(gpu, monkeypatch, n):
     r1 = gpu.Context(cp, 1).plan_report()["radix_a"]
     r2 = gpu.Context(cp, 1).plan_report()["radix_a"]
     assert r1 == r2 and r1 in (8, 16)
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 512])
+def test_pass_c_carrying_pass_a_is_bit_identical(gpu, monkeypatch, n):
+    """FP32 grids up to 512: inside r2d3c_advance each substep's pass C
+    launch also runs the next substep's pass A on the column pairs it has
+    just updated (plan_report "fused_ca"; each advance call starts with one
+    separate pass A).  With R2D3C_FUSE_CA=0 pass A keeps its own launch.
+    The states and times are bit-identical over several calls, in both dt
+    modes, with closure tendencies on, under forced pass C shapes (two CTAs
+    per column pair, teams of 2 and 4 groups)."""
+    import torch
+    from rot2d3c_gb300.closure import set_tendency
+    cp, ps, vz, fp, fz = _case(n, 17)
+    rng = np.random.default_rng(n)
+    tend = torch.from_numpy((float(n) * rng.standard_normal((n, n, 2))).astype(np.float32)).cuda()
+    shapes = (None, "0,1,0,1,2", "0,1,0,0,2,4", "0,1,0,0,2,2") if n >= 256 else (None,)
+    for forced in shapes:
+        outs = []
+        for fuse in ("1", "0"):
+            monkeypatch.setenv("R2D3C_FUSE_CA", fuse)
+            monkeypatch.setenv("R2D3C_PASSC", "per_column_pair")
+            if forced:
+                monkeypatch.setenv("R2D3C_GROUPS", forced)
+            else:
+                monkeypatch.delenv("R2D3C_GROUPS", raising=False)
+            c = gpu.Context(cp, 1)
+            assert c.plan_report()["fused_ca"] == (fuse == "1")
+            c.set_state(ps, vz)
+            c.set_forcing(fp, fz)
+            c.set_time(0.0)
+            t1, _ = c.advance(3, gpu.DT_CFL, 0.5)
+            t2, _ = c.advance(2, gpu.DT_FIXED, 1e-4)
+            set_tendency(c, tend)
+            t3, _ = c.advance(2, gpu.DT_CFL, 0.5)
+            set_tendency(c, None)
+            outs.append((c.get_state(), (t1, t2, t3)))
+            c.destroy()
+        (s1, times1), (s0, times0) = outs
+        assert times1 == times0, forced
+        for u, v in zip(s1, s0):
+            np.testing.assert_array_equal(u, v)
+    monkeypatch.setenv("R2D3C_FUSE_CA", "2")
+    with pytest.raises(gpu.R2D3CError):
+        gpu.Context(cp, 1)
