@@ -656,12 +656,18 @@ def run_closure(small=False, cfg=None):
     the loop against the plain and hyperviscous coarse solvers and the
     filtered DNS over the same physical time.  The gain is the DNS's GPU
     seconds over the LES's for that time."""
-    from rot2d3c_gb300.les import run_experiment
+    from rot2d3c_gb300.les import run_experiment, step_timing
     cfg = cfg or (CLOSURE_SMALL if small else CLOSURE)
     r = run_experiment(**cfg)
     tr = r["training"]
     nshow = 16
+    # GPU time per coarse step of each LES schedule (graph replay, CUDA events)
+    steps_us = step_timing(nc=cfg["nc"], steps=200, nu=cfg["nu"], hnu=cfg["hnu"], omega=cfg["omega"],
+                           cfl=cfg["cfl"])
     return {"les_vs_dns_gain": r["les"]["gain"], "unit": "DNS GPU-s / LES GPU-s (same physical time)",
+            "step_us": dict({k: round(v, 2) for k, v in steps_us.items()},
+                            note="us per coarse step: plain solver; network before every step, every second "
+                                 "step, one step behind beside the step (overlap)"),
             "dns": r["dns"], "les": r["les"], "spectrum_error": r["spectrum_error"],
             "spectrum_error_per_start": r["spectrum_error_per_start"], "skill": r["skill"],
             "spectra_shells_0_15": {k: [float(f"{x:.4g}") for x in v[:nshow]] for k, v in r["spectra"].items()},

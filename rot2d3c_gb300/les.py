@@ -329,6 +329,44 @@ def evaluate(ds, net, les_steps=4000, spec_every=50, fallback_nn=4, bands=("near
             "spectra": spectra_mean}
 
 
+def step_timing(nc=256, steps=200, seed=1, nu=2e-5, hnu=1.0, omega=1.0, cfl=0.5):
+    """GPU time per coarse step (CUDA events on the context's stream, graph
+    replay after a warm-up) of the plain solver and of the LES with the
+    network before every step, before every second step, and one step
+    behind beside the step (closure_advance's overlap), at nc^2 with the
+    closure experiment's coefficients and band rule and a freshly created
+    network (the timing does not depend on its weights).  Returns
+    {"plain": us, "every_1": us, "every_2": us, "overlap": us}."""
+    import torch
+    steps = max(2, steps // 2 * 2)
+    ps, vz, fp, fz = _setup_run(nc, seed)
+    p = make_params(n=nc, nu=nu, nuv=nu, hnu=hnu, hnuv=hnu, nn=1, mm=2, nnv=1, mmv=2, omega=omega, iflow=0, cfl=cfl)
+    c = Context(p, FP32)
+    c.set_state(ps, vz)
+    c.set_forcing(fp, fz)
+    c.set_time(0.0)
+    net = CNN(nc, nc, 1, seed)
+    set_band(c, band_weights("near_cutoff", nc // 3, nc // 2 + 1))
+    st = torch.cuda.ExternalStream(c.stream())
+    runs = {"plain": lambda k: c.advance(k, DT_CFL, cfl),
+            "every_1": lambda k: closure_advance(c, net, k, DT_CFL, cfl),
+            "every_2": lambda k: closure_advance(c, net, k, DT_CFL, cfl, every=2),
+            "overlap": lambda k: closure_advance(c, net, k, DT_CFL, cfl, overlap=True)}
+    out = {}
+    for name, run in runs.items():
+        run(10)  # capture and warm-up
+        c.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        run(steps)
+        e1.record(st)
+        e1.synchronize()
+        out[name] = 1e3 * e0.elapsed_time(e1) / steps
+    net.destroy()
+    c.destroy()
+    return out
+
+
 def run_experiment(nf=2048, nc=256, omega=1.0, nu=2e-5, nsnap=1000, snap_every=10, spinup=2000,
                    train_steps=3000, batch=32, lr=1e-3, les_steps=4000, cfl=0.5, seed=1,
                    fallback_nn=4, spec_every=50, hnu=0.1, starts=4, band="near_cutoff", compare_bands=(), every=1,
