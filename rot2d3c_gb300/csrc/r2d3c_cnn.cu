@@ -336,13 +336,19 @@ k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float*
   unsigned* s_tmem = reinterpret_cast<unsigned*>(s_bar + 1);
   float* s_bias = reinterpret_cast<float*>(s_bar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // Launched with programmatic stream serialisation: the next convolution
+  // may start its prologue (weights, bias, barrier, tensor memory) as this
+  // one's CTAs leave; it reads this one's outputs only after
+  // griddepcontrol.wait, which returns once this grid has completed and
+  // its writes are visible.  Nothing before that wait reads what a
+  // preceding kernel writes or writes what it reads.
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   // the bias (the last layer's has only its cout_store real channels)
   if (tid < COUT) s_bias[tid] = bias && tid < cout_store ? bias[tid] : 0.f;
   // weights, already in the K-major UMMA layout: unit (kc, n) = k 8kc..8kc+7 of column n
   for (int i = tid; i < TC::W_UNITS; i += kTcThreads) tc_cp16(s_w + i, wt + (size_t)i * 8);
   tc_commit();
   int t = blockIdx.x;
-  tc_stage_halo<CIN>(s_halo, in, t, ntiles, H, W);
   const unsigned bar = smem_u32(s_bar);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
@@ -357,6 +363,8 @@ k_conv_tc(const bf16* __restrict__ in, const bf16* __restrict__ wt, const float*
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const unsigned tmem = *s_tmem;
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");  // the input activations are complete
+  tc_stage_halo<CIN>(s_halo, in, t, ntiles, H, W);
   const int tiles_x = W / kTcPix;
   unsigned phase = 0;
   for (int it = 0; t < ntiles; t += gridDim.x, ++it) {
@@ -724,8 +732,20 @@ template <int CIN, int COUT>
 void conv_tc_launch(const bf16* in, const bf16* w, const float* b, int B, int H, int W, float* y, bf16* a, int act,
                     int cout_store, int ctas, int* err, cudaStream_t st) {
   const int tiles = B * H * (W / kTcPix);
-  k_conv_tc<CIN, COUT><<<std::min(tiles, ctas), kTcThreads, TcConv<CIN, COUT>::SMEM, st>>>(
-      in, w, b, H, W, tiles, y, a, act, cout_store, err);
+  // programmatic stream serialisation: the prologue overlaps the preceding
+  // kernel's tail (k_conv_tc waits before its first read of `in`)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(std::min(tiles, ctas));
+  cfg.blockDim = dim3(kTcThreads);
+  cfg.dynamicSmemBytes = TcConv<CIN, COUT>::SMEM;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cuda_check(cudaLaunchKernelEx(&cfg, k_conv_tc<CIN, COUT>, in, w, b, H, W, tiles, y, a, act, cout_store, err),
+             "k_conv_tc");
 }
 template <int CIN, int COUT>
 int resident_tc_ctas() {
