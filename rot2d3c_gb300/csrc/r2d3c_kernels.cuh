@@ -641,7 +641,7 @@ k_passB_split(const cpx<T>* __restrict__ tf, cpx<T>* __restrict__ pb, int kxo, D
   tf += blockIdx.y * bs.tf;
   pb += blockIdx.y * bs.pb;
   cfl_enc += blockIdx.y * kScalStride;
-  R2D3C_SMEM_DECL
+  extern __shared__ __align__(16) unsigned char smraw_[];
   const int j = threadIdx.x / TPF, lane = threadIdx.x % TPF;
   cpx<T>* sm = reinterpret_cast<cpx<T>*>(smraw_ + (size_t)j * F::SMEM_BYTES);
   cpx<T>* res = reinterpret_cast<cpx<T>*>(smraw_ + 3 * F::SMEM_BYTES);  // [pair j][row t][x]
