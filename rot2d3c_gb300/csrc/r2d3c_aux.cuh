@@ -29,6 +29,15 @@ struct Scale8 {
   double v[8];
 };
 
+// Row i (kx index) and column j (ky index) of element idx of a spectral
+// plane [kx][ky] of n columns: n is a power of two in every engine, so a
+// shift and a mask take the place of a 64-bit division (an emulated
+// instruction sequence per element)
+__device__ __forceinline__ void plane_ij(size_t idx, int n, int& i, int& j) {
+  i = (int)(idx >> (__ffs(n) - 1));
+  j = (int)(idx & (size_t)(n - 1));
+}
+
 template <typename T>
 __global__ void k_specop(const cpx<T>* __restrict__ a, cpx<T>* __restrict__ b, DevGrid gd, int op,
                          double s) {
@@ -36,7 +45,8 @@ __global__ void k_specop(const cpx<T>* __restrict__ a, cpx<T>* __restrict__ b, D
   const T sc = (T)s;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
+    int i, j;
+    plane_ij(idx, gd.n, i, j);
     const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
     const int k2 = kx * kx + ky * ky;
     const cpx<T> x = a[idx];
@@ -134,7 +144,8 @@ k_halfplane_sums(const cpx<T>* __restrict__ p0, const cpx<T>* __restrict__ p1,
   const size_t total = (size_t)gd.nh * gd.n;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
+    int i, j;
+    plane_ij(idx, gd.n, i, j);
     const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
     const int k2 = kx * kx + ky * ky;
     const double ka2 = (double)k2;
@@ -404,7 +415,8 @@ __global__ void k_scale_mask2(cpx<T>* a, cpx<T>* b, DevGrid gd, double sa, doubl
   const size_t total = (size_t)gd.nh * gd.n;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / gd.n), j = (int)(idx % gd.n);
+    int i, j;
+    plane_ij(idx, gd.n, i, j);
     const int kx = kx_of(i, gd.n), ky = ky_of(j, gd.n);
     const int k2 = kx * kx + ky * ky;
     const bool in = k2 <= gd.kmaxi && k2 >= 1;
@@ -429,7 +441,8 @@ __global__ void k_ci_base(const cpx<T>* __restrict__ src, cpx<T>* __restrict__ d
   const int n = gd.n;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / n), j = (int)(idx % n);
+    int i, j;
+    plane_ij(idx, n, i, j);
     const int kx = kx_of(i, n), ky = ky_of(j, n);
     const double ka2 = (double)(kx * kx + ky * ky);
     const bool band = ka2 <= hi && ka2 >= lo;
@@ -481,7 +494,8 @@ __global__ void k_coarsen(const cpx<T>* __restrict__ fine, int nf, cpx<T>* __res
   const size_t total = (size_t)gc.nh * gc.n;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / gc.n), j = (int)(idx % gc.n);
+    int i, j;
+    plane_ij(idx, gc.n, i, j);
     const int ky = ky_of(j, gc.n);
     const int k2 = i * i + ky * ky;
     cpx<T> v = czero<T>();
@@ -503,7 +517,8 @@ __global__ void k_refine(const cpx<T>* __restrict__ coarse, int nc, cpx<T>* __re
   const size_t total = (size_t)gf.nh * gf.n;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / gf.n), j = (int)(idx % gf.n);
+    int i, j;
+    plane_ij(idx, gf.n, i, j);
     const int ky = ky_of(j, gf.n);
     cpx<T> v = czero<T>();
     if (i < nc / 2 && ky < nc / 2 && -ky < nc / 2) {
@@ -537,7 +552,8 @@ __global__ void k_shell_weight2(const cpx<T>* a_in, const cpx<T>* b_in, cpx<T>* 
       b[i] = v;
       continue;
     }
-    const int kx = (int)(i / gd.n), j = (int)(i % gd.n);
+    int kx, j;
+    plane_ij(i, gd.n, kx, j);
     const int ky = ky_of(j, gd.n);
     // (2b-1)^2 < 4 ka2 < (2b+1)^2  <=>  b = (isqrt(4 ka2) + 1) / 2
     const int bsh = (int)((isqrt_ll(4LL * ((long long)kx * kx + (long long)ky * ky)) + 1) / 2);
