@@ -548,7 +548,8 @@ def run_ensemble(args, torch, rank=0, world=1):
            "runs": len(runs), "groups": [list(g) for g in ENSEMBLE["groups"]], "steps_per_run": K,
            "seconds": el, "gpu_launches": ens.kernel_launches() - l0, "dtype": "f32 (FP64 reductions)",
            "ranks": world, "partition": "runs dealt by cost n^2 log2 n (LPT), diagnostics gathered on the host",
-           "plan": {str(g["n"]): plan_summary_dict(g["plan"]) for g in ens.plan_report()},
+           "plan": {str(g["n"]): dict(plan_summary_dict(g["plan"]), policy=g["plan"].get("policy"))
+                    for g in ens.plan_report()},
            "budget_residual": {"median": float(np.median(resid)), "max": float(resid.max()),
                                "worst_run": {"index": worst, "n": runs[worst][0],
                                              "omega": runs[worst][1]["omega"]},

@@ -753,12 +753,14 @@ int r2d3c_ensemble_create(int ngroups, const int* n, const int* runs, const r2d3
   for (auto& j : e->joins) cuda_check(cudaEventCreateWithFlags(&j, cudaEventDisableTiming), "cudaEventCreate");
   if (ngroups > 1) {
     // The graph runs the size groups side by side, where launch shapes timed
-    // alone are no guide: the whole step is timed under both plan policies
-    // (fixed dt on the new ensemble's zero state, which stays zero) and the
-    // faster is kept; the runs' times are reset afterwards.
+    // alone are no guide: the whole step is timed under each plan policy
+    // (per-pass best; full CTAs or persistent; persistent passes B and C
+    // wherever they exist) with fixed dt on the new ensemble's zero state,
+    // which stays zero, and the fastest is kept; the runs' times are reset
+    // afterwards.
     double best = 0.0;
     int pick = 0;
-    for (int pol = 0; pol < 2; ++pol) {
+    for (int pol = 0; pol < 3; ++pol) {
       for (auto& g : e->groups) {
         g.eng->set_plan_policy(pol);
         g.eng->set_dt_all(1e-9);

@@ -1396,8 +1396,11 @@ class EngineT final : public IEngine {
   // whose graphs run the groups side by side, where a flood of small CTAs
   // from one group measured slower than full ones): pass A with the
   // config's groups per CTA and all six fields in one CTA, passes B and C
-  // with the config's groups per CTA or persistent.  The environment
-  // overrides (R2D3C_PASSB, R2D3C_PASSC, R2D3C_GROUPS) apply to both.
+  // with the config's groups per CTA or persistent.  Policy 2: as policy 1,
+  // with passes B and C persistent wherever that form exists (a pass C
+  // that is faster alone with one CTA per column pair measured slower side
+  // by side with the other groups).  The environment overrides
+  // (R2D3C_PASSB, R2D3C_PASSC, R2D3C_GROUPS) apply to all three.
   void choose_plan() {
     if (const char* e = std::getenv("R2D3C_FUSE_CA")) {
       if (std::strcmp(e, "0") != 0 && std::strcmp(e, "1") != 0) throw Error(kEINVAL, "R2D3C_FUSE_CA must be 0 or 1");
@@ -1458,6 +1461,10 @@ class EngineT final : public IEngine {
         auto ok = [&](const TuneRec& r) { return pol == 0 || r.mode == 1 || (r.mode == 0 && r.grid == GB); };
         const size_t pick0 = argmin(t, [&](const TuneRec& r) { return r.mode == 0 && ok(r); });
         size_t pick = argmin(t, ok);
+        if (pol == 2) {  // the persistent form wherever it exists
+          const size_t pp = argmin(t, [](const TuneRec& r) { return r.mode == 1; });
+          if (pp < t.size()) pick = pp;
+        }
         // env=<pair_name>|persistent overrides the measured choice
         // (persistent where it exists: FP32, n = 512 .. 4096)
         if (const char* force = std::getenv(env)) {
@@ -1494,7 +1501,7 @@ class EngineT final : public IEngine {
     });
   }
   void set_plan_policy(int policy) override {
-    if (policy != 0 && policy != 1) throw Error(kEINVAL, "plan policy must be 0 or 1");
+    if (policy < 0 || policy > 2) throw Error(kEINVAL, "plan policy must be 0, 1 or 2");
     policy_ = policy;
     choose_plan();
   }
