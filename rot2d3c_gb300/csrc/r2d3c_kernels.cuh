@@ -1265,7 +1265,7 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
       const int fb = chunk == 1 ? 4 : 0, fe = chunk == 0 ? 4 : 6;
       const int rounds = (fe - fb + W - 1) / W;
       const size_t plane = (size_t)gd.M * N;
-      cpx<T>* asm_ = smbase_ + (size_t)g * PS::GROUP_ELEMS;  // this group's transform buffers
+      cpx<T>* tsm = smbase_ + (size_t)g * PS::GROUP_ELEMS;  // this group's transform buffers
 #pragma unroll 1
       for (int r = 0; r < rounds; ++r) {
         const int f = fb + member + r * W;
@@ -1289,7 +1289,7 @@ k_passC(const cpx<T>* __restrict__ pb, const cpx<T>* c1in, const cpx<T>* c2in,
             a[t][q] = mkc<T>(-k * x.y, k * x.x);
           }
         }
-        F::template run<+1>(a, lane, asm_, twa);
+        F::template run<+1>(a, lane, tsm, twa);
         // lanes (2p, 2p+1) hold rows y = 2p, 2p+1 of columns kx0, kx0+1: one
         // swap, then each lane writes one column's row pair (16 bytes)
         const bool odd = lane & 1;
