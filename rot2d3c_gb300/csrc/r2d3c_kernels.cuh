@@ -958,6 +958,9 @@ __device__ __forceinline__ void rk_load(RkIn<T>& r, size_t idx, const cpx<T>* c1
 
 // New C1 (rk_apply1) and C2 (rk_apply2) of one element
 // (Rot2D3C.para.f90:580-599); zero outside the retained disc and at k = 0.
+// Both components are divided by the same implicit divisor: one reciprocal
+// and two products (within an ulp of the two quotients; an FP64 division
+// is a long sequence on the FP64 pipe, which binds the FP64 path).
 // The two are independent: C1 needs C2's input (the Coriolis term 2 Omega
 // d_y C2) and [psi, -k^2 psi], C2 needs C1's input and [psi, vz].
 template <typename T>
@@ -970,7 +973,8 @@ __device__ __forceinline__ cpx<T> rk_apply1(const RkIn<T>& r, const cpx<T> c5, i
   const T tmp3 = (T)1 + (nu * powi(ka2, sc.nn) + hnu * powi(tmp2, sc.mm)) * tmp1;
   const T u1x = r.p0.x + ((-c5.x + w2 * C4.x) * tmp2 + r.f0.x) * tmp1;
   const T u1y = r.p0.y + ((-c5.y + w2 * C4.y) * tmp2 + r.f0.y) * tmp1;
-  return mkc<T>(u1x / tmp3, u1y / tmp3);
+  const T r3 = (T)1 / tmp3;
+  return mkc<T>(u1x * r3, u1y * r3);
 }
 template <typename T>
 __device__ __forceinline__ cpx<T> rk_apply2(const RkIn<T>& r, const cpx<T> c6, int kyi, int k2, const StepCoef& sc,
@@ -982,7 +986,8 @@ __device__ __forceinline__ cpx<T> rk_apply2(const RkIn<T>& r, const cpx<T> c6, i
   const T tmp3v = (T)1 + (nuv * powi(ka2, sc.nnv) + hnuv * powi(tmp2, sc.mmv)) * tmp1;
   const T u2x = r.v0.x + (c6.x + w2 * C3.x + r.g0.x) * tmp1;
   const T u2y = r.v0.y + (c6.y + w2 * C3.y + r.g0.y) * tmp1;
-  return mkc<T>(u2x / tmp3v, u2y / tmp3v);
+  const T r3v = (T)1 / tmp3v;
+  return mkc<T>(u2x * r3v, u2y * r3v);
 }
 template <typename T>
 __device__ __forceinline__ void rk_apply(const RkIn<T>& r, const cpx<T> c5, const cpx<T> c6, int kyi, int k2,
