@@ -67,7 +67,8 @@ def parse():
     ap.add_argument("--no-closure", action="store_true")
     ap.add_argument("--no-precision-study", action="store_true", help="skip the 8192^2 FP32-vs-FP64 leg")
     ap.add_argument("--closure-full", action="store_true",
-                    help="also run the closure experiment at BASELINE config 5's stated sizes (several minutes)")
+                    help="also run the full-size closure experiment: 2048^2 DNS at nu = 5e-6, 2000 snapshots, "
+                         "20k Adam steps, 5000 LES steps, Omega 1 and 10 (several minutes)")
     ap.add_argument("--e2e-steps", type=int, default=20, help="steps of the host round-trip e2e leg")
     ap.add_argument("--loop-steps", type=int, default=200, help="steps of the main-loop e2e leg (0: skip)")
     ap.add_argument("--oracle-steps", type=int, default=100,
@@ -638,8 +639,9 @@ CLOSURE = dict(nf=2048, nc=256, omega=1.0, nu=2e-5, hnu=1.0, nsnap=1000, snap_ev
 CLOSURE_SMALL = dict(CLOSURE, nf=512, nc=128, nu=2e-4, nsnap=64, snap_every=5, spinup=200, train_steps=40,
                      les_steps=200, spec_every=20, every=1)
 
-# BASELINE config 5 as stated (nu = 5e-6, 2000 snapshots, 20k Adam steps of
-# batch 32 at lr 1e-3, 5000 LES steps), once per Omega in {1, 10}; the
+# The full-size closure experiment (2048^2 DNS -> 256^2 LES, nu = 5e-6, 2000
+# snapshots, 20k Adam steps of batch 32 at lr 1e-3, 5000 LES steps), once per
+# Omega in {1, 10}; the
 # reference's default hypoviscosity (parameter.inp: hnu = 1, mm = 2) keeps
 # the forced flow statistically steady.  Several minutes: --closure-full.
 CLOSURE_FULL = dict(nf=2048, nc=256, nu=5e-6, hnu=1.0, nsnap=2000, snap_every=20, spinup=10000,
@@ -647,7 +649,7 @@ CLOSURE_FULL = dict(nf=2048, nc=256, nu=5e-6, hnu=1.0, nsnap=2000, snap_every=20
 
 
 def run_closure_full():
-    """BASELINE config 5 at its stated sizes for Omega = 1 and Omega = 10."""
+    """The full-size closure experiment for Omega = 1 and Omega = 10."""
     return {f"omega_{om:g}": run_closure(cfg=dict(CLOSURE_FULL, omega=om)) for om in (1.0, 10.0)}
 
 
