@@ -468,7 +468,7 @@ class EngineT final : public IEngine {
     if (!graph_ || !key.same(gkey_)) {
       if (graph_) cudaGraphExecDestroy(graph_);
       graph_ = nullptr;
-      cudaGraph_t g;
+      cudaGraph_t g = nullptr;
       const int before = launches_;
       cuda_check(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal), "BeginCapture");
       cudaStream_t main = st_;
