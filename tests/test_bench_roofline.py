@@ -60,3 +60,34 @@ def test_roofline_object():
     assert r64["fp64_pipe"]["achieved"] == pytest.approx(fB / 5.23e-3 / 1e12)
     assert r64["fp64_pipe"]["frac"] == pytest.approx(fB / 5.23e-3 / 1e12 / 1.2546)
     assert 0.55 < r64["fp64_pipe"]["frac"] < 0.7
+
+
+def _samples(t, e, inj, diss):
+    import numpy as np
+    S = np.zeros((len(t), 1, 30))
+    S[:, 0, 0] = t
+    S[:, 0, 1] = S[:, 0, 2] = e           # (E + Ez) / 2 = e
+    S[:, 0, 3] = inj
+    S[:, 0, 5] = diss
+    return S
+
+
+def test_budget_residual_closes_and_shows_the_sampling_error():
+    """The ensemble leg's energy-budget residual |mean(dE/dt - (inj -
+    diss))| / mean|inj|: zero for a budget that closes exactly, and, for
+    an energy exchange oscillating at frequency w with a closed budget,
+    small when sampled densely but large when the centred difference spans
+    a sizeable part of a period (the every-tenth-step sampling)."""
+    import numpy as np
+    t = np.linspace(0.0, 1.0, 101)
+    lin = bench.budget_residuals(_samples(t, 1.0 + 0.3 * t, np.full_like(t, 1.0), np.full_like(t, 0.7)))
+    assert lin[0] == pytest.approx(0.0, abs=1e-12)
+    w = 2 * np.pi * 40.0                      # a run of 0.45 periods of the exchange
+    dense = np.linspace(0.0, 0.0113, 113)
+    coarse = dense[::10]                      # every tenth sample
+    res = []
+    for tt in (dense, coarse):
+        e = 1.0 + 0.05 * np.sin(w * tt)
+        inj = 1.0 + 0.05 * w * np.cos(w * tt)   # inj - diss = dE/dt exactly
+        res.append(bench.budget_residuals(_samples(tt, e, inj, np.full_like(tt, 1.0)))[0])
+    assert res[0] < 1e-4 and res[1] > 50 * res[0]
