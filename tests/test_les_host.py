@@ -50,9 +50,9 @@ def test_device_shell_rule_equals_the_reference_rule():
     """The kernels that weight tendencies per shell take the shell as
     b = (isqrt(4 ka2) + 1) / 2 in integers, i.e. (2b-1)^2 < 4 ka2 < (2b+1)^2;
     the reference bins by kmn = int(sqrt(ka2) + .5)
-    (pseudospec2D_Rot2D3C.f90:615-712).  They agree for every ka2 a grid up
-    to 8192^2 holds, and shell_index (the host's map of a plane) is the
-    same rule."""
+    (pseudospec2D_Rot2D3C.f90:615-712).  They agree for every ka2 up to
+    2e5 and every 997th up to the largest of an 8192^2 grid, and
+    shell_index (the host's map of a plane) is the same rule."""
     ka2 = np.arange(0, 2 * 4096 * 4096 + 1, 997, dtype=np.int64)
     ka2 = np.concatenate([ka2, np.arange(0, 200000, dtype=np.int64)])
     dev = (np.array([math.isqrt(int(4 * k)) for k in ka2]) + 1) // 2
